@@ -1,0 +1,160 @@
+/*
+ * smcgpu.h -- C ABI of the GB300 nested-SMC fault-geometry / slip inversion.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an
+ * int32_t status (SMCGPU_OK = 0) and never exits, stops or traps.  Arrays are
+ * in the reference's Fortran layouts (column-major, first index fastest), so a
+ * Fortran caller passes its own arrays through ISO_C_BINDING unchanged; the
+ * `bind(C)` interface module is shown in INTEGRATION.md.  Host pointers are
+ * owned by the caller and not retained past a call.  One context drives one
+ * GPU; calls on a context must be serialised by the caller.
+ *
+ * Reference interfaces replaced (paths inside KaiNakao/smc_inversion_fort):
+ *   smcgpu_set_data            main.f90:254-307 + init.f90:5-119 (data, Sigma_SAR^-1)
+ *   smcgpu_greens_batch        gfunc.f90:242-348 calc_greens_func, batched over theta
+ *   smcgpu_fault_likelihood_batch
+ *                              smc_fault.f90:66-292 fault_calc_likelihood, batched
+ *                              (discretize_fault, gen_laplacian, calc_greens_func,
+ *                              slip_smc_exec for every theta in one call)
+ *   smcgpu_fault_smc_exec      smc_fault.f90:785-1075 fault_smc_exec
+ *   smcgpu_resample_counts     smc_slip.f90:572-589 / smc_fault.f90:572-590
+ *   smcgpu_qsort_              sort.cpp:3-7 qsort_ (same symbol shape)
+ */
+#ifndef SMCGPU_H
+#define SMCGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SMCGPU_MAX_PLANES 8
+
+/* status codes (returned) */
+#define SMCGPU_OK            0
+#define SMCGPU_ERR_ARG      -1
+#define SMCGPU_ERR_CUDA     -2
+#define SMCGPU_ERR_NODATA   -3
+#define SMCGPU_ERR_MEMORY   -4
+#define SMCGPU_ERR_STATE    -5
+
+/* per-theta status bits (status_out of the likelihood calls) */
+#define SMCGPU_ST_BISECT_CAP   1   /* gamma bisection hit its iteration cap           */
+#define SMCGPU_ST_STAGE_CAP    2   /* > max_stages tempering stages; neglog = 1e10    */
+#define SMCGPU_ST_NONFINITE    4   /* non-finite evidence or Cholesky failure          */
+#define SMCGPU_ST_NEWTON_CAP   8   /* inverse-CDF Newton loop hit 100 iterations       */
+#define SMCGPU_ST_REFLECT_CAP 16   /* reflection loop hit its cap                      */
+#define SMCGPU_ST_TUNE_COUNT  32   /* step-size resampling count != N                  */
+
+/* theta layouts */
+#define SMCGPU_LAYOUT_TRACE          0  /* [ymin ymax (x_i y_i)_{i<nplane} dip_1..n la2 ls_sar ls_gnss] (init.f90:152-167) */
+#define SMCGPU_LAYOUT_TRACE_FIXBEND  1  /* [ymin ymax y_i.. dip_1..n la2 ls_sar ls_gnss] (init.f90:135-150)              */
+#define SMCGPU_LAYOUT_RECT           2  /* [x y top length width strike dip la2 (ls_sar ls_gnss)] one buried rectangle    */
+
+/* slip bases */
+#define SMCGPU_BASIS_NODAL  0  /* bilinear nodal slip, reference (gfunc.f90:158-171) */
+#define SMCGPU_BASIS_PATCH  1  /* patch-constant slip                                */
+
+/* precisions */
+#define SMCGPU_PREC_FP64   0   /* FP64 everywhere, reference operation order          */
+#define SMCGPU_PREC_FP32   1   /* Green's build only: FP32 arithmetic, float output    */
+#define SMCGPU_PREC_MIXED  2   /* nested SMC: FP32 leapfrog, FP64 likelihood/evidence  */
+
+typedef struct smcgpu_config {
+    int32_t layout;
+    int32_t basis;
+    int32_t nplane;
+    int32_t nxi[SMCGPU_MAX_PLANES];
+    int32_t neta[SMCGPU_MAX_PLANES];
+    double xbend[SMCGPU_MAX_PLANES];
+    double xmin, xmax, zmin;       /* trace extent and fault bottom (km, zmin < 0)       */
+    int32_t nquad;                 /* Gauss points per patch direction (reference: 2)    */
+    int32_t rect_hyper;            /* LAYOUT_RECT: theta carries log sigma2 sar/gnss     */
+    double alpha;                  /* medium constant (reference: 2/3)                   */
+    double max_slip;               /* slip box [0, max_slip] (m)                         */
+    int32_t nparticle_slip;        /* inner particles                                    */
+    int32_t ntau;                  /* leapfrog steps (reference: 50)                     */
+    int32_t tuning_factor;         /* every k-th parent tunes the step (reference: 5)    */
+    int32_t max_stages;            /* inner stage cap (reference: 200)                   */
+    double cv_inner;               /* inner weight CV target (reference: 2.0)            */
+    double cv_outer;               /* outer weight CV target (reference: 0.2)            */
+    double sar_corr_len;           /* InSAR covariance range km (reference: 10)          */
+    int32_t precision;             /* SMCGPU_PREC_FP64 or SMCGPU_PREC_MIXED              */
+    int32_t device;                /* CUDA device ordinal                                */
+} smcgpu_config;
+
+typedef struct smcgpu_ctx smcgpu_ctx;
+
+/* Fill *cfg with the reference's constants (one plane, nodal basis, 2x2
+ * Gauss points, alpha = 2/3, ntau = 50, tuning factor 5, 200 stages, CV 2 and
+ * 0.2, 10 km SAR range, FP64). */
+int32_t smcgpu_default_config(smcgpu_config *cfg);
+
+/* Create a context on cfg->device.  Replaces the allocation block of
+ * main.f90:349-390; the mesh pattern is fixed here. */
+int32_t smcgpu_create(const smcgpu_config *cfg, smcgpu_ctx **out);
+int32_t smcgpu_destroy(smcgpu_ctx *ctx);
+
+/* Observations in the reference's arrays (read_observation2, init.f90:24-80):
+ * obs_points(2,nobs), obs_unitvec(3,nobs), obs_sigma(nobs), dvec(nobs);
+ * nsar_index(npath+1) is the reference's 1-based path start table; GNSS rows
+ * follow the SAR rows in triples.  Sigma_SAR^-1 (init.f90:82-119) is built
+ * here in FP64.  Copies everything to the device. */
+int32_t smcgpu_set_data(smcgpu_ctx *ctx, int32_t nobs, const double *obs_points, const double *obs_unitvec,
+                        const double *obs_sigma, const double *dvec, int32_t npath,
+                        const int32_t *nsar_index, int32_t ngnss);
+
+/* Work on the caller's CUDA stream (cudaStream_t passed as void*); NULL
+ * selects the context's own stream. */
+int32_t smcgpu_set_stream(smcgpu_ctx *ctx, void *stream);
+
+/* Dimensions: ndim_fault, D = 2*ndof (nodal) or 2*npatch, nobs, nrow_l. */
+int32_t smcgpu_dims(const smcgpu_ctx *ctx, int32_t *ndim_fault, int32_t *D, int32_t *nobs, int32_t *nrow_l);
+
+/* Green's matrices for n_theta geometries: gmat(nobs, D, n_theta), the
+ * reference's gmat(nobs, 2*ndof) per theta (gfunc.f90:242-348).  precision
+ * SMCGPU_PREC_FP64 writes double, SMCGPU_PREC_FP32 writes float.
+ * _batch takes host buffers (copies inside the call); _batch_dev takes device
+ * pointers already in HBM. */
+int32_t smcgpu_greens_batch(smcgpu_ctx *ctx, int32_t n_theta, const double *theta, int32_t precision,
+                            void *gmat);
+int32_t smcgpu_greens_batch_dev(smcgpu_ctx *ctx, int32_t n_theta, const double *theta_dev,
+                                int32_t precision, void *gmat_dev);
+
+/* Nested evaluation -log Z(theta) for n_theta geometries (fault_calc_likelihood,
+ * smc_fault.f90:66-292).  Every evaluation draws from the Philox4x64-10 stream
+ * keyed by (seed, streams[i]); status_out gets SMCGPU_ST_* bits; a stage-cap
+ * hit returns neglog = 1e10 as the reference does (smc_slip.f90:1557-1560). */
+int32_t smcgpu_fault_likelihood_batch(smcgpu_ctx *ctx, int32_t n_theta, const double *theta, uint64_t seed,
+                                      const uint64_t *streams, double *neglog_out, int32_t *status_out);
+int32_t smcgpu_fault_likelihood_batch_dev(smcgpu_ctx *ctx, int32_t n_theta, const double *theta_dev,
+                                          uint64_t seed, const uint64_t *streams_dev, double *neglog_dev,
+                                          int32_t *status_dev);
+
+/* The full outer SMC (fault_smc_exec, smc_fault.f90:785-1075) with a uniform
+ * prior box range(2, ndim_fault).  particles_out(ndim_fault, nparticle) and
+ * likelihood_out(nparticle) receive the final population.  When output_dir
+ * is not NULL, the reference's per-stage CSV files <iter>.csv are written
+ * there (smc_fault.f90:923-936, 1054-1067). */
+int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, int32_t nparticle, uint64_t seed,
+                              const char *output_dir, double *particles_out, double *likelihood_out,
+                              double *evidence_out, int32_t *nstage_out);
+
+/* Residual-systematic resampling counts on the device (smc_slip.f90:572-589).
+ * u0 is the binary128 uniform of random_number_correction_dd carried as a
+ * double-double (u0_hi + u0_lo exactly).  counts match the reference's
+ * binary128 recurrence bit for bit. */
+int32_t smcgpu_resample_counts(smcgpu_ctx *ctx, const double *weights, int32_t n, double u0_hi, double u0_lo,
+                               int32_t *counts);
+
+/* Drop-in for sort.cpp:3-7 qsort_(arr, index, n): orders the 1-based index[]
+ * by arr[index-1] descending with the same std::sort comparator. */
+void smcgpu_qsort_(int32_t *arr, int32_t *index, int32_t *n);
+
+/* Last error message of the context (or of the last create call when ctx is NULL). */
+const char *smcgpu_last_error(const smcgpu_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

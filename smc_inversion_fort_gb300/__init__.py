@@ -1,0 +1,225 @@
+"""GB300-native nested-SMC fault-geometry and slip inversion.
+
+Python mirror of the reference's operator interface for the hot path
+(KaiNakao/smc_inversion_fort: fault_calc_likelihood, calc_greens_func,
+fault_smc_exec, the resampling step and sort.cpp's qsort_) over the C ABI in
+include/smcgpu.h.  The CUDA library must be built (see build.py); every call
+goes to the GPU and fails loudly when the library or a device is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .configs import SmcSettings, preset  # noqa: F401
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libsmcgpu.so")
+
+MAX_PLANES = 8
+LAYOUT_TRACE, LAYOUT_TRACE_FIXBEND, LAYOUT_RECT = 0, 1, 2
+BASIS_NODAL, BASIS_PATCH = 0, 1
+PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
+ST_BISECT_CAP, ST_STAGE_CAP, ST_NONFINITE, ST_NEWTON_CAP, ST_REFLECT_CAP, ST_TUNE_COUNT = 1, 2, 4, 8, 16, 32
+
+
+class SmcConfig(C.Structure):
+    """ctypes mirror of smcgpu_config."""
+    _fields_ = [
+        ("layout", C.c_int32), ("basis", C.c_int32), ("nplane", C.c_int32),
+        ("nxi", C.c_int32 * MAX_PLANES), ("neta", C.c_int32 * MAX_PLANES),
+        ("xbend", C.c_double * MAX_PLANES),
+        ("xmin", C.c_double), ("xmax", C.c_double), ("zmin", C.c_double),
+        ("nquad", C.c_int32), ("rect_hyper", C.c_int32),
+        ("alpha", C.c_double), ("max_slip", C.c_double),
+        ("nparticle_slip", C.c_int32), ("ntau", C.c_int32), ("tuning_factor", C.c_int32),
+        ("max_stages", C.c_int32),
+        ("cv_inner", C.c_double), ("cv_outer", C.c_double), ("sar_corr_len", C.c_double),
+        ("precision", C.c_int32), ("device", C.c_int32),
+    ]
+
+
+_lib = None
+
+
+def load_library() -> C.CDLL:
+    """Load libsmcgpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run smc_inversion_fort_gb300.build.build() first")
+    lib = C.CDLL(LIB_PATH)
+    P = C.POINTER
+    d, i32, u64, vp = C.c_double, C.c_int32, C.c_uint64, C.c_void_p
+    sig = {
+        "smcgpu_default_config": (i32, [P(SmcConfig)]),
+        "smcgpu_create": (i32, [P(SmcConfig), P(vp)]),
+        "smcgpu_destroy": (i32, [vp]),
+        "smcgpu_set_data": (i32, [vp, i32, vp, vp, vp, vp, i32, vp, i32]),
+        "smcgpu_set_stream": (i32, [vp, vp]),
+        "smcgpu_dims": (i32, [vp, P(i32), P(i32), P(i32), P(i32)]),
+        "smcgpu_greens_batch": (i32, [vp, i32, vp, i32, vp]),
+        "smcgpu_greens_batch_dev": (i32, [vp, i32, vp, i32, vp]),
+        "smcgpu_fault_likelihood_batch": (i32, [vp, i32, vp, u64, vp, vp, vp]),
+        "smcgpu_fault_likelihood_batch_dev": (i32, [vp, i32, vp, u64, vp, vp, vp]),
+        "smcgpu_fault_smc_exec": (i32, [vp, vp, i32, u64, C.c_char_p, vp, vp, vp, vp]),
+        "smcgpu_resample_counts": (i32, [vp, vp, i32, d, d, vp]),
+        "smcgpu_qsort_": (None, [vp, vp, vp]),
+        "smcgpu_last_error": (C.c_char_p, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+EXPORTED_SYMBOLS = [
+    "smcgpu_default_config", "smcgpu_create", "smcgpu_destroy", "smcgpu_set_data", "smcgpu_set_stream",
+    "smcgpu_dims", "smcgpu_greens_batch", "smcgpu_greens_batch_dev", "smcgpu_fault_likelihood_batch",
+    "smcgpu_fault_likelihood_batch_dev", "smcgpu_fault_smc_exec", "smcgpu_resample_counts", "smcgpu_qsort_",
+    "smcgpu_last_error",
+]
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class SmcError(RuntimeError):
+    pass
+
+
+def make_config(s: SmcSettings, precision: int = PREC_FP64, device: int = 0) -> SmcConfig:
+    cfg = SmcConfig()
+    load_library().smcgpu_default_config(C.byref(cfg))
+    cfg.layout, cfg.basis, cfg.nplane = s.layout, s.basis, s.nplane
+    for k in range(s.nplane):
+        cfg.nxi[k], cfg.neta[k] = s.nxi[k], s.neta[k]
+    for k, v in enumerate(s.xbend):
+        cfg.xbend[k] = v
+    cfg.xmin, cfg.xmax, cfg.zmin = s.xmin, s.xmax, s.zmin
+    cfg.nquad, cfg.rect_hyper, cfg.alpha, cfg.max_slip = s.nquad, s.rect_hyper, s.alpha, s.max_slip
+    cfg.nparticle_slip, cfg.ntau, cfg.tuning_factor, cfg.max_stages = s.nparticle_slip, s.ntau, s.tuning_factor, s.max_stages
+    cfg.cv_inner, cfg.cv_outer, cfg.sar_corr_len = s.cv_inner, s.cv_outer, s.sar_corr_len
+    cfg.precision, cfg.device = precision, device
+    return cfg
+
+
+class SmcGpu:
+    """One GPU context: observations resident in HBM, batched calls.
+
+    Method names follow the reference routines they replace.
+    """
+
+    def __init__(self, settings: SmcSettings, precision: int = PREC_FP64, device: int = 0):
+        self.lib = load_library()
+        self.settings = settings
+        self.cfg = make_config(settings, precision, device)
+        h = C.c_void_p()
+        rc = self.lib.smcgpu_create(C.byref(self.cfg), C.byref(h))
+        if rc != 0:
+            raise SmcError(f"smcgpu_create failed ({rc}): {self.lib.smcgpu_last_error(None).decode()}")
+        self.h = h
+        self.nobs = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.smcgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            raise SmcError(f"{what} failed ({rc}): {self.lib.smcgpu_last_error(self.h).decode()}")
+
+    def dims(self):
+        a, b, c, d = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(self.lib.smcgpu_dims(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)), "dims")
+        return {"ndim_fault": a.value, "D": b.value, "nobs": c.value, "nrow_l": d.value}
+
+    def set_data(self, obs):
+        """obs: dict with obs_points (nobs,2), obs_unitvec (nobs,3), obs_sigma, dvec, nsar_index
+        (1-based, npath+1), ngnss -- the arrays of read_observation2 (init.f90:24-80)."""
+        self._obs = {k: np.ascontiguousarray(v) for k, v in obs.items() if isinstance(v, np.ndarray)}
+        pts = np.ascontiguousarray(obs["obs_points"], dtype=np.float64)
+        e = np.ascontiguousarray(obs["obs_unitvec"], dtype=np.float64)
+        sg = np.ascontiguousarray(obs["obs_sigma"], dtype=np.float64)
+        dv = np.ascontiguousarray(obs["dvec"], dtype=np.float64)
+        idx = np.ascontiguousarray(obs.get("nsar_index", np.array([1], np.int32)), dtype=np.int32)
+        npath = len(idx) - 1
+        self._keep = (pts, e, sg, dv, idx)
+        self._check(self.lib.smcgpu_set_data(self.h, len(dv), _ptr(pts), _ptr(e), _ptr(sg), _ptr(dv), npath,
+                                             _ptr(idx), int(obs["ngnss"])), "set_data")
+        self.nobs = len(dv)
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self.lib.smcgpu_set_stream(self.h, stream_handle or None), "set_stream")
+
+    # calc_greens_func, batched (gfunc.f90:242-348)
+    def calc_greens_func(self, theta: np.ndarray, precision: int = PREC_FP64, out: np.ndarray | None = None):
+        th = np.ascontiguousarray(np.atleast_2d(theta), dtype=np.float64)
+        dm = self.dims()
+        dt = np.float32 if precision == PREC_FP32 else np.float64
+        if out is None:
+            out = np.empty((th.shape[0], dm["D"], dm["nobs"]), dtype=dt)
+        self._check(self.lib.smcgpu_greens_batch(self.h, th.shape[0], _ptr(th), precision, _ptr(out)), "greens_batch")
+        return out
+
+    def greens_dev(self, n_theta: int, theta_ptr: int, gmat_ptr: int, precision: int = PREC_FP64):
+        self._check(self.lib.smcgpu_greens_batch_dev(self.h, n_theta, theta_ptr, precision, gmat_ptr), "greens_batch_dev")
+
+    # fault_calc_likelihood, batched (smc_fault.f90:66-292)
+    def fault_calc_likelihood(self, theta: np.ndarray, seed: int, streams=None):
+        th = np.ascontiguousarray(np.atleast_2d(theta), dtype=np.float64)
+        n = th.shape[0]
+        st = np.ascontiguousarray(np.arange(n, dtype=np.uint64) if streams is None else streams, dtype=np.uint64)
+        neglog = np.empty(n, np.float64)
+        status = np.empty(n, np.int32)
+        self._check(self.lib.smcgpu_fault_likelihood_batch(self.h, n, _ptr(th), seed, _ptr(st), _ptr(neglog),
+                                                           _ptr(status)), "fault_likelihood_batch")
+        return neglog, status
+
+    def fault_likelihood_dev(self, n, theta_ptr, seed, streams_ptr, neglog_ptr, status_ptr):
+        self._check(self.lib.smcgpu_fault_likelihood_batch_dev(self.h, n, theta_ptr, seed, streams_ptr, neglog_ptr,
+                                                               status_ptr), "fault_likelihood_batch_dev")
+
+    # fault_smc_exec (smc_fault.f90:785-1075)
+    def fault_smc_exec(self, range_: np.ndarray, nparticle: int, seed: int, output_dir: str | None = None):
+        rg = np.ascontiguousarray(range_, dtype=np.float64)
+        nd = self.dims()["ndim_fault"]
+        parts = np.empty((nparticle, nd), np.float64)
+        lik = np.empty(nparticle, np.float64)
+        ev = C.c_double()
+        ns = C.c_int32()
+        od = output_dir.encode() if output_dir else None
+        self._check(self.lib.smcgpu_fault_smc_exec(self.h, _ptr(rg), nparticle, seed, od, _ptr(parts), _ptr(lik),
+                                                   C.byref(ev), C.byref(ns)), "fault_smc_exec")
+        return parts, lik, ev.value, ns.value
+
+    # slip_resample_particles / fault_resample_particles (binary128-exact counts)
+    def resample_counts(self, weights: np.ndarray, u0_hi: float, u0_lo: float):
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        out = np.empty(len(w), np.int32)
+        self._check(self.lib.smcgpu_resample_counts(self.h, _ptr(w), len(w), u0_hi, u0_lo, _ptr(out)),
+                    "resample_counts")
+        return out
+
+
+def qsort_(arr: np.ndarray, index: np.ndarray) -> None:
+    """sort.cpp's qsort_: sorts the 1-based index array in place."""
+    lib = load_library()
+    a = np.ascontiguousarray(arr, dtype=np.int32)
+    if not (index.flags["C_CONTIGUOUS"] and index.dtype == np.int32):
+        raise ValueError("index must be a contiguous int32 array")
+    n = C.c_int32(len(index))
+    lib.smcgpu_qsort_(_ptr(a), _ptr(index), C.byref(n))

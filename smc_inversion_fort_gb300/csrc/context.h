@@ -1,0 +1,57 @@
+// Context object behind the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/smcgpu.h"
+#include "devbuf.h"
+#include "kernels.h"
+#include "mesh.h"
+
+struct smcgpu_ctx {
+    smcgpu_config cfg;
+    smc::MeshPattern mesh;
+    smc::MeshDev md{};
+    cudaStream_t own_stream = nullptr, copy_stream = nullptr, stream = nullptr;
+    std::string err;
+    bool has_data = false;
+    // host copy of the observation layout
+    int nobs = 0, nsar = 0, ngnss = 0, npath = 0, nstation = 0;
+    std::vector<int> nsar_index0;  // zero-based path starts, npath+1
+    std::vector<double> sar_whiten;   // per path lower-triangular W with W^T W = Sigma^-1 (col-major)
+    std::vector<long long> sar_off;
+    std::vector<double> dvec_h;
+    double dsd_sar = 0.0, dsd_gnss = 0.0;  // whitened data norms (without sigma2 scalings)
+
+    // pattern tables
+    smc::DevBuf<int> d_dof_of_node, d_l_col, d_l_plane, d_lt_row, d_lt_plane, d_ll_ptr, d_ll_col;
+    smc::DevBuf<signed char> d_l_k, d_lt_k;
+    // observations
+    smc::DevBuf<double> d_st_x, d_st_y, d_obs_e, d_obs_sigma, d_dvec, d_sar_w, d_dx, d_roww;
+    smc::DevBuf<int> d_st_row, d_st_nrow, d_nsar_index;
+    smc::DevBuf<long long> d_sar_off;
+
+    // batch work buffers
+    smc::DevBuf<double> d_theta;
+    smc::DevBuf<smc::PlaneGeom> d_planes;
+    smc::DevBuf<char> d_gchunk[2];
+    smc::DevBuf<double> d_gmat, d_gw, d_A, d_b, d_dsd, d_lval, d_ltval, d_llval;
+    smc::DevBuf<smc::ThetaAux> d_aux;
+    smc::DevBuf<double> d_neglog;
+    smc::DevBuf<int> d_status;
+    smc::DevBuf<unsigned long long> d_streams;
+    smc::DevBuf<double> d_w;
+    smc::DevBuf<int> d_counts, d_flag;
+    cudaEvent_t ev_done[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
+
+    int fail(int code, const std::string &msg) {
+        err = msg;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char *where) {
+        err = std::string(where) + ": " + cudaGetErrorString(e);
+        return SMCGPU_ERR_CUDA;
+    }
+};
