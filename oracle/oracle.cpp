@@ -8,8 +8,6 @@
 // the CUDA path also uses, so both can be driven by identical draws.
 #include "oracle.h"
 
-#include <quadmath.h>
-
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -20,7 +18,18 @@
 #include <omp.h>
 #endif
 
+// real(16): IEEE binary128.  AArch64 Linux's long double is binary128
+// (software arithmetic in libgcc); on x86-64 GCC's __float128 + libquadmath.
+#if defined(__aarch64__)
+typedef long double quad;
+static inline quad q_floor(quad x) { return floorl(x); }
+static inline quad q_log(quad x) { return logl(x); }
+#else
+#include <quadmath.h>
 typedef __float128 quad;
+static inline quad q_floor(quad x) { return floorq(x); }
+static inline quad q_log(quad x) { return logq(x); }
+#endif
 
 // ---------------------------------------------------------------------------
 // Random stream (replaces random_number / random_number_correction,
@@ -1065,7 +1074,7 @@ static void resample_q(const double *w, int n, int count_n, quad u, int32_t *a) 
     quad dn = (quad)count_n;
     u = u / dn;
     for (int i = 0; i < n; ++i) {
-        a[i] = (int32_t)floorq(((quad)w[i] - u) * dn) + 1;
+        a[i] = (int32_t)q_floor(((quad)w[i] - u) * dn) + 1;
         u = u + (quad)a[i] / dn - (quad)w[i];
     }
 }
@@ -1261,8 +1270,8 @@ static double inner_smc(Inner &in, double *particles, double *Ls, double *Ps, or
                 quad dm = 0;
                 for (int k = 0; k < N; ++k) dm = dm + (quad)dtau_ls[k];
                 dm = dm / (quad)N;
-                log_dtau_upper = (double)(logq(dm) + (quad)log(5.0));
-                log_dtau_lower = (double)(logq(dm) - (quad)log(5.0));
+                log_dtau_upper = (double)(q_log(dm) + (quad)log(5.0));
+                log_dtau_lower = (double)(q_log(dm) - (quad)log(5.0));
             }
         }
         // slip_hmc_sampling (:591-730)

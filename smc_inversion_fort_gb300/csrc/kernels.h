@@ -24,8 +24,10 @@ cudaError_t launch_setup(const MeshDev &m, int n_theta, const double *theta_dev,
                          double *lval, double *ltval, double *llval, ThetaAux *aux, cudaStream_t s);
 
 // gram.cu: A = G^T Sigma^-1 G, b = G^T Sigma^-1 d, dsd (smc_slip.f90:1347-1443)
-cudaError_t launch_gram(const MeshDev &m, int n_theta, const double *gmat, const ThetaAux *aux, double *A,
-                        double *b, double *dsd, double *work, size_t work_elems, cudaStream_t s);
+// gw: n_theta*D*nsar work buffer for the whitened InSAR rows (unused without InSAR)
+cudaError_t launch_gram(const MeshDev &m, int n_theta, const double *gmat, const double *roww, const double *dx,
+                        const ThetaAux *aux, double dsd_sar, double dsd_gnss, double *A, double *b, double *dsd,
+                        double *gw, cudaStream_t s);
 
 // resample.cu
 cudaError_t launch_resample_counts(const double *w, int n, double u_hi, double u_lo, int *counts, int *flag,
