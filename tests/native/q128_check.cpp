@@ -6,7 +6,7 @@ typedef long double f128;
 #define floorq floorl
 #else
 #include <quadmath.h>
-typedef f128 f128;
+typedef __float128 f128;
 #endif
 #include <cstdio>
 #include <cstring>
