@@ -184,7 +184,10 @@ def gb300_arm(args):
     dm = g.dims()
     D, nobs, n = dm["D"], dm["nobs"], args.n_theta
     entries = n * nobs * D
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated (non-default) stream: the library launches on it and the
+    # CUDA events below are recorded on it
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     g.set_stream(stream.cuda_stream)
     dth = torch.from_numpy(th).to(dev)
     out = torch.empty((n, D, nobs), dtype=torch.float64, device=dev)

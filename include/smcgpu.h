@@ -105,7 +105,8 @@ int32_t smcgpu_set_data(smcgpu_ctx *ctx, int32_t nobs, const double *obs_points,
                         const int32_t *nsar_index, int32_t ngnss);
 
 /* Work on the caller's CUDA stream (cudaStream_t passed as void*); NULL
- * selects the context's own stream. */
+ * selects the context's own non-blocking stream; the legacy default stream is
+ * selected with cudaStreamLegacy ((void*)1). */
 int32_t smcgpu_set_stream(smcgpu_ctx *ctx, void *stream);
 
 /* Dimensions: ndim_fault, D = 2*ndof (nodal) or 2*npatch, nobs, nrow_l. */
@@ -130,6 +131,21 @@ int32_t smcgpu_fault_likelihood_batch(smcgpu_ctx *ctx, int32_t n_theta, const do
 int32_t smcgpu_fault_likelihood_batch_dev(smcgpu_ctx *ctx, int32_t n_theta, const double *theta_dev,
                                           uint64_t seed, const uint64_t *streams_dev, double *neglog_dev,
                                           int32_t *status_dev);
+
+/* Diagnostic variant of smcgpu_fault_likelihood_batch (host buffers): also
+ * returns the number of tempering stages per theta and the stage-by-stage
+ * tempering exponent and -log evidence increment, gamma_trace /
+ * inc_trace (max_stages+2, n_theta), zero past the last stage. */
+int32_t smcgpu_fault_likelihood_trace(smcgpu_ctx *ctx, int32_t n_theta, const double *theta, uint64_t seed,
+                                      const uint64_t *streams, double *neglog_out, int32_t *status_out,
+                                      int32_t *nstage_out, double *gamma_trace, double *inc_trace);
+
+/* One nested evaluation that also returns the final slip population, the
+ * data behind the reference's flag_output = 1 slip file (smc_slip.f90:1632-1660):
+ * particles_out(D, nparticle_slip), likelihood_out and prior_out(nparticle_slip). */
+int32_t smcgpu_fault_likelihood_posterior(smcgpu_ctx *ctx, const double *theta, uint64_t seed, uint64_t stream,
+                                          double *neglog_out, int32_t *status_out, double *particles_out,
+                                          double *likelihood_out, double *prior_out);
 
 /* The full outer SMC (fault_smc_exec, smc_fault.f90:785-1075) with a uniform
  * prior box range(2, ndim_fault).  particles_out(ndim_fault, nparticle) and

@@ -65,6 +65,8 @@ def load_library() -> C.CDLL:
         "smcgpu_greens_batch_dev": (i32, [vp, i32, vp, i32, vp]),
         "smcgpu_fault_likelihood_batch": (i32, [vp, i32, vp, u64, vp, vp, vp]),
         "smcgpu_fault_likelihood_batch_dev": (i32, [vp, i32, vp, u64, vp, vp, vp]),
+        "smcgpu_fault_likelihood_trace": (i32, [vp, i32, vp, u64, vp, vp, vp, vp, vp, vp]),
+        "smcgpu_fault_likelihood_posterior": (i32, [vp, vp, u64, u64, vp, vp, vp, vp, vp]),
         "smcgpu_fault_smc_exec": (i32, [vp, vp, i32, u64, C.c_char_p, vp, vp, vp, vp]),
         "smcgpu_resample_counts": (i32, [vp, vp, i32, d, d, vp]),
         "smcgpu_qsort_": (None, [vp, vp, vp]),
@@ -81,7 +83,8 @@ def load_library() -> C.CDLL:
 EXPORTED_SYMBOLS = [
     "smcgpu_default_config", "smcgpu_create", "smcgpu_destroy", "smcgpu_set_data", "smcgpu_set_stream",
     "smcgpu_dims", "smcgpu_greens_batch", "smcgpu_greens_batch_dev", "smcgpu_fault_likelihood_batch",
-    "smcgpu_fault_likelihood_batch_dev", "smcgpu_fault_smc_exec", "smcgpu_resample_counts", "smcgpu_qsort_",
+    "smcgpu_fault_likelihood_batch_dev", "smcgpu_fault_likelihood_trace", "smcgpu_fault_likelihood_posterior",
+    "smcgpu_fault_smc_exec", "smcgpu_resample_counts", "smcgpu_qsort_",
     "smcgpu_last_error",
 ]
 
@@ -188,6 +191,29 @@ class SmcGpu:
         self._check(self.lib.smcgpu_fault_likelihood_batch(self.h, n, _ptr(th), seed, _ptr(st), _ptr(neglog),
                                                            _ptr(status)), "fault_likelihood_batch")
         return neglog, status
+
+    def fault_likelihood_trace(self, theta: np.ndarray, seed: int, streams=None):
+        th = np.ascontiguousarray(np.atleast_2d(theta), dtype=np.float64)
+        n = th.shape[0]
+        ms = self.settings.max_stages + 2
+        st = np.ascontiguousarray(np.arange(n, dtype=np.uint64) if streams is None else streams, dtype=np.uint64)
+        neglog, status, nstage = np.empty(n), np.empty(n, np.int32), np.empty(n, np.int32)
+        gam, inc = np.zeros((n, ms)), np.zeros((n, ms))
+        self._check(self.lib.smcgpu_fault_likelihood_trace(self.h, n, _ptr(th), seed, _ptr(st), _ptr(neglog),
+                                                           _ptr(status), _ptr(nstage), _ptr(gam), _ptr(inc)),
+                    "fault_likelihood_trace")
+        return {"neglog": neglog, "status": status, "nstage": nstage,
+                "gamma": [gam[i, :nstage[i]] for i in range(n)], "neglog_inc": [inc[i, :nstage[i]] for i in range(n)]}
+
+    def fault_likelihood_posterior(self, theta: np.ndarray, seed: int, stream: int = 0):
+        th = np.ascontiguousarray(theta, dtype=np.float64)
+        N, D = self.settings.nparticle_slip, self.dims()["D"]
+        nl, stt = C.c_double(), C.c_int32()
+        parts, L, P = np.empty((N, D)), np.empty(N), np.empty(N)
+        self._check(self.lib.smcgpu_fault_likelihood_posterior(self.h, _ptr(th), seed, stream, C.byref(nl),
+                                                               C.byref(stt), _ptr(parts), _ptr(L), _ptr(P)),
+                    "fault_likelihood_posterior")
+        return {"neglog": nl.value, "status": stt.value, "particles": parts, "likelihood": L, "prior": P}
 
     def fault_likelihood_dev(self, n, theta_ptr, seed, streams_ptr, neglog_ptr, status_ptr):
         self._check(self.lib.smcgpu_fault_likelihood_batch_dev(self.h, n, theta_ptr, seed, streams_ptr, neglog_ptr,

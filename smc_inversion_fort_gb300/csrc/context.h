@@ -42,6 +42,8 @@ struct smcgpu_ctx {
     smc::DevBuf<double> d_neglog;
     smc::DevBuf<int> d_status;
     smc::DevBuf<unsigned long long> d_streams;
+    smc::DevBuf<double> d_parts, d_parts_new, d_dbuf, d_trace;
+    smc::DevBuf<int> d_ibuf, d_nstage_tmp, d_nstage;
     smc::DevBuf<double> d_w;
     smc::DevBuf<int> d_counts, d_flag;
     cudaEvent_t ev_done[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};

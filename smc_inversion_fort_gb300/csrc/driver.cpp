@@ -1,5 +1,7 @@
-// C ABI entry points of the nested likelihood, the outer SMC and the
-// stand-alone resampling primitive.
+// C ABI entry points of the nested likelihood (fault_calc_likelihood), the
+// outer SMC (fault_smc_exec) and the stand-alone resampling primitive.
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -8,12 +10,115 @@
 #include <vector>
 
 #include "context.h"
+#include "inner.h"
 
-#define CU(call, where)                                  \
-    do {                                                 \
-        cudaError_t e_ = (call);                         \
+#define CU(call, where)                                          \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
         if (e_ != cudaSuccess) return ctx->cuda_fail(e_, where); \
     } while (0)
+
+namespace {
+
+struct NestedOpts {
+    double *trace_gamma = nullptr, *trace_inc = nullptr;  // device, [n][max_stages+2]
+    int *nstage = nullptr;                                // device [n]
+    double *particles_out = nullptr;                      // host [N][D] of theta 0 (single-theta call)
+    double *lik_out = nullptr, *prior_out = nullptr;      // host [N]
+};
+
+int next_pow2(int n) {
+    int p = 1;
+    while (p < n) p <<= 1;
+    return p;
+}
+
+size_t bytes_per_theta(const smcgpu_ctx *ctx) {
+    const smc::MeshPattern &p = ctx->mesh;
+    size_t D = p.D, N = ctx->cfg.nparticle_slip, NP2 = next_pow2((int)N);
+    size_t b = D * ctx->nobs * 8 + D * std::max(ctx->nsar, 0) * 8 + D * D * 8 + D * 8 + 8;
+    b += (size_t)p.nrow * 9 * 8 + D * 9 * 8 + p.ll_col.size() * 8 + sizeof(smc::ThetaAux);
+    b += 2 * N * D * 8 + 9 * N * 8 + 4 * NP2 * 4 + p.nplane * sizeof(smc::PlaneGeom) + 64;
+    return b;
+}
+
+// Runs the nested evaluation for n thetas already on the device, in chunks.
+int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed, const unsigned long long *streams_dev,
+                 double *neglog_dev, int *status_dev, const NestedOpts &opt) {
+    const smc::MeshPattern &pm = ctx->mesh;
+    const int D = pm.D, N = ctx->cfg.nparticle_slip, NP2 = next_pow2(N), nd = pm.ndim_fault;
+    cudaStream_t s = ctx->stream;
+    size_t per = bytes_per_theta(ctx);
+    size_t budget = (size_t)48 << 30;
+    size_t freeb = 0, totb = 0;
+    if (cudaMemGetInfo(&freeb, &totb) == cudaSuccess) budget = std::min(budget, freeb / 2);
+    int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)n, budget / per));
+    CU(ctx->d_planes.ensure((size_t)chunk * pm.nplane), "alloc");
+    CU(ctx->d_gmat.ensure((size_t)chunk * D * ctx->nobs), "alloc gmat");
+    CU(ctx->d_gw.ensure((size_t)chunk * D * std::max(ctx->nsar, 1)), "alloc gw");
+    CU(ctx->d_A.ensure((size_t)chunk * D * D), "alloc A");
+    CU(ctx->d_b.ensure((size_t)chunk * D), "alloc b");
+    CU(ctx->d_dsd.ensure((size_t)chunk), "alloc dsd");
+    CU(ctx->d_lval.ensure((size_t)chunk * pm.nrow * 9), "alloc lval");
+    CU(ctx->d_ltval.ensure((size_t)chunk * D * 9), "alloc ltval");
+    CU(ctx->d_llval.ensure((size_t)chunk * std::max<size_t>(pm.ll_col.size(), 1)), "alloc llval");
+    CU(ctx->d_aux.ensure((size_t)chunk), "alloc aux");
+    CU(ctx->d_parts.ensure((size_t)chunk * N * D), "alloc particles");
+    CU(ctx->d_parts_new.ensure((size_t)chunk * N * D), "alloc particles");
+    CU(ctx->d_dbuf.ensure((size_t)chunk * 9 * N), "alloc dbuf");
+    CU(ctx->d_ibuf.ensure((size_t)chunk * 4 * NP2), "alloc ibuf");
+    CU(ctx->d_nstage_tmp.ensure((size_t)chunk), "alloc");
+    for (int t0 = 0; t0 < n; t0 += chunk) {
+        int nb = std::min(chunk, n - t0);
+        const double *th = theta_dev + (size_t)t0 * nd;
+        CU(smc::launch_planes(ctx->md, nb, th, ctx->d_planes.p, s), "planes kernel");
+        CU(smc::launch_greens(ctx->md, nb, ctx->d_planes.p, SMCGPU_PREC_FP64, ctx->d_gmat.p, s), "greens kernel");
+        CU(smc::launch_setup(ctx->md, nb, th, ctx->d_planes.p, ctx->d_lval.p, ctx->d_ltval.p, ctx->d_llval.p,
+                             ctx->d_aux.p, s), "setup kernel");
+        CU(smc::launch_gram(ctx->md, nb, ctx->d_gmat.p, ctx->d_roww.p, ctx->d_dx.p, ctx->d_aux.p, ctx->dsd_sar,
+                            ctx->dsd_gnss, ctx->d_A.p, ctx->d_b.p, ctx->d_dsd.p, ctx->d_gw.p, s), "gram kernel");
+        CU(cudaMemsetAsync(status_dev + t0, 0, (size_t)nb * sizeof(int), s), "memset");
+        CU(cudaMemsetAsync(ctx->d_ibuf.p, 0, (size_t)nb * 4 * NP2 * sizeof(int), s), "memset");
+        smc::InnerArgs a{};
+        a.n_theta = nb; a.N = N; a.NP2 = NP2; a.D = D;
+        a.mixed = ctx->cfg.precision == SMCGPU_PREC_MIXED;
+        a.ntau = ctx->cfg.ntau; a.tf = ctx->cfg.tuning_factor; a.max_stages = ctx->cfg.max_stages;
+        a.cv = ctx->cfg.cv_inner; a.max_slip = ctx->cfg.max_slip; a.seed = seed;
+        a.streams = streams_dev + t0;
+        a.A = ctx->d_A.p; a.b = ctx->d_b.p; a.dsd = ctx->d_dsd.p; a.lval = ctx->d_lval.p; a.llval = ctx->d_llval.p;
+        a.aux = ctx->d_aux.p;
+        a.parts = ctx->d_parts.p; a.parts_new = ctx->d_parts_new.p; a.dbuf = ctx->d_dbuf.p; a.ibuf = ctx->d_ibuf.p;
+        a.neglog = neglog_dev + t0; a.status = status_dev + t0;
+        a.nstage = opt.nstage ? opt.nstage + t0 : ctx->d_nstage_tmp.p;
+        a.trace_gamma = opt.trace_gamma ? opt.trace_gamma + (size_t)t0 * (a.max_stages + 2) : nullptr;
+        a.trace_inc = opt.trace_inc ? opt.trace_inc + (size_t)t0 * (a.max_stages + 2) : nullptr;
+        CU(smc::launch_gibbs(ctx->md, a, s), "gibbs kernel");
+        const char *why = nullptr;
+        cudaError_t e = smc::launch_inner(ctx->md, a, s, &why);
+        if (e != cudaSuccess) {
+            if (why) return ctx->fail(SMCGPU_ERR_ARG, why);
+            return ctx->cuda_fail(e, "inner kernel");
+        }
+        if (opt.particles_out && t0 == 0) {
+            CU(cudaMemcpyAsync(opt.particles_out, ctx->d_parts.p, (size_t)N * D * sizeof(double),
+                               cudaMemcpyDeviceToHost, s), "copy particles");
+            CU(cudaMemcpyAsync(opt.lik_out, ctx->d_dbuf.p, (size_t)N * sizeof(double), cudaMemcpyDeviceToHost, s),
+               "copy");
+            CU(cudaMemcpyAsync(opt.prior_out, ctx->d_dbuf.p + N, (size_t)N * sizeof(double), cudaMemcpyDeviceToHost,
+                               s), "copy");
+        }
+    }
+    return SMCGPU_OK;
+}
+
+int check_ready(smcgpu_ctx *ctx) {
+    if (!ctx->has_data) return ctx->fail(SMCGPU_ERR_NODATA, "set_data not called");
+    if (ctx->cfg.precision != SMCGPU_PREC_FP64 && ctx->cfg.precision != SMCGPU_PREC_MIXED)
+        return ctx->fail(SMCGPU_ERR_ARG, "nested evaluation needs precision FP64 or MIXED");
+    return SMCGPU_OK;
+}
+
+}  // namespace
 
 extern "C" int32_t smcgpu_resample_counts(smcgpu_ctx *ctx, const double *weights, int32_t n, double u0_hi,
                                           double u0_lo, int32_t *counts) {
@@ -35,23 +140,313 @@ extern "C" int32_t smcgpu_resample_counts(smcgpu_ctx *ctx, const double *weights
 extern "C" int32_t smcgpu_fault_likelihood_batch_dev(smcgpu_ctx *ctx, int32_t n_theta, const double *theta_dev,
                                                      uint64_t seed, const uint64_t *streams_dev, double *neglog_dev,
                                                      int32_t *status_dev) {
-    (void)n_theta; (void)theta_dev; (void)seed; (void)streams_dev; (void)neglog_dev; (void)status_dev;
     if (!ctx) return SMCGPU_ERR_ARG;
-    return ctx->fail(SMCGPU_ERR_STATE, "nested likelihood not available in this build");
+    int r = check_ready(ctx);
+    if (r) return r;
+    if (n_theta < 0 || (n_theta > 0 && (!theta_dev || !streams_dev || !neglog_dev || !status_dev)))
+        return ctx->fail(SMCGPU_ERR_ARG, "fault_likelihood: bad arguments");
+    if (n_theta == 0) return SMCGPU_OK;
+    CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+    return nested_batch(ctx, n_theta, theta_dev, seed, (const unsigned long long *)streams_dev, neglog_dev,
+                        status_dev, NestedOpts());
+}
+
+static int likelihood_host(smcgpu_ctx *ctx, int n, const double *theta, uint64_t seed, const uint64_t *streams,
+                           double *neglog_out, int32_t *status_out, int32_t *nstage_out, double *gamma_trace,
+                           double *inc_trace, double *particles_out, double *lik_out, double *prior_out) {
+    int r = check_ready(ctx);
+    if (r) return r;
+    if (n < 0 || (n > 0 && (!theta || !streams || !neglog_out || !status_out)))
+        return ctx->fail(SMCGPU_ERR_ARG, "fault_likelihood: bad arguments");
+    if (n == 0) return SMCGPU_OK;
+    CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+    const int nd = ctx->mesh.ndim_fault, ms = ctx->cfg.max_stages + 2;
+    cudaStream_t s = ctx->stream;
+    CU(ctx->d_theta.upload(theta, (size_t)n * nd, s), "upload theta");
+    CU(ctx->d_streams.upload((const unsigned long long *)streams, n, s), "upload streams");
+    CU(ctx->d_neglog.ensure(n), "alloc");
+    CU(ctx->d_status.ensure(n), "alloc");
+    NestedOpts opt;
+    if (nstage_out || gamma_trace || inc_trace) {
+        CU(ctx->d_nstage.ensure(n), "alloc");
+        CU(ctx->d_trace.ensure((size_t)2 * n * ms), "alloc");
+        CU(cudaMemsetAsync(ctx->d_trace.p, 0, (size_t)2 * n * ms * sizeof(double), s), "memset");
+        opt.nstage = ctx->d_nstage.p;
+        opt.trace_gamma = ctx->d_trace.p;
+        opt.trace_inc = ctx->d_trace.p + (size_t)n * ms;
+    }
+    opt.particles_out = particles_out;
+    opt.lik_out = lik_out;
+    opt.prior_out = prior_out;
+    r = nested_batch(ctx, n, ctx->d_theta.p, seed, ctx->d_streams.p, ctx->d_neglog.p, ctx->d_status.p, opt);
+    if (r) return r;
+    CU(cudaMemcpyAsync(neglog_out, ctx->d_neglog.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
+    CU(cudaMemcpyAsync(status_out, ctx->d_status.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+    if (nstage_out)
+        CU(cudaMemcpyAsync(nstage_out, ctx->d_nstage.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+    if (gamma_trace)
+        CU(cudaMemcpyAsync(gamma_trace, ctx->d_trace.p, (size_t)n * ms * sizeof(double), cudaMemcpyDeviceToHost, s),
+           "copy");
+    if (inc_trace)
+        CU(cudaMemcpyAsync(inc_trace, ctx->d_trace.p + (size_t)n * ms, (size_t)n * ms * sizeof(double),
+                           cudaMemcpyDeviceToHost, s), "copy");
+    CU(cudaStreamSynchronize(s), "sync");
+    return SMCGPU_OK;
 }
 
 extern "C" int32_t smcgpu_fault_likelihood_batch(smcgpu_ctx *ctx, int32_t n_theta, const double *theta, uint64_t seed,
                                                  const uint64_t *streams, double *neglog_out, int32_t *status_out) {
-    (void)n_theta; (void)theta; (void)seed; (void)streams; (void)neglog_out; (void)status_out;
     if (!ctx) return SMCGPU_ERR_ARG;
-    return ctx->fail(SMCGPU_ERR_STATE, "nested likelihood not available in this build");
+    return likelihood_host(ctx, n_theta, theta, seed, streams, neglog_out, status_out, nullptr, nullptr, nullptr,
+                           nullptr, nullptr, nullptr);
 }
 
-extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, int32_t nparticle, uint64_t seed,
+extern "C" int32_t smcgpu_fault_likelihood_trace(smcgpu_ctx *ctx, int32_t n_theta, const double *theta, uint64_t seed,
+                                                 const uint64_t *streams, double *neglog_out, int32_t *status_out,
+                                                 int32_t *nstage_out, double *gamma_trace, double *inc_trace) {
+    if (!ctx) return SMCGPU_ERR_ARG;
+    return likelihood_host(ctx, n_theta, theta, seed, streams, neglog_out, status_out, nstage_out, gamma_trace,
+                           inc_trace, nullptr, nullptr, nullptr);
+}
+
+extern "C" int32_t smcgpu_fault_likelihood_posterior(smcgpu_ctx *ctx, const double *theta, uint64_t seed,
+                                                     uint64_t stream, double *neglog_out, int32_t *status_out,
+                                                     double *particles_out, double *likelihood_out,
+                                                     double *prior_out) {
+    if (!ctx) return SMCGPU_ERR_ARG;
+    if (!particles_out || !likelihood_out || !prior_out) return ctx->fail(SMCGPU_ERR_ARG, "posterior: null output");
+    return likelihood_host(ctx, 1, theta, seed, &stream, neglog_out, status_out, nullptr, nullptr, nullptr,
+                           particles_out, likelihood_out, prior_out);
+}
+
+// ---------------------------------------------------------------------------
+// Outer SMC (fault_smc_exec, smc_fault.f90:785-1075), uniform prior box,
+// driven from the host; every batch of nested evaluations is one device
+// pipeline (Green's build, Gram, Gibbs init, inner SMC) over all thetas.
+// ---------------------------------------------------------------------------
+static int chol_lower_inplace(std::vector<double> &a, int n) {
+    for (int j = 0; j < n; ++j) {
+        double d = a[(size_t)j * n + j];
+        for (int k = 0; k < j; ++k) d -= a[(size_t)k * n + j] * a[(size_t)k * n + j];
+        if (!(d > 0.0)) return j + 1;
+        d = std::sqrt(d);
+        a[(size_t)j * n + j] = d;
+        for (int i = j + 1; i < n; ++i) {
+            double v = a[(size_t)j * n + i];
+            for (int k = 0; k < j; ++k) v -= a[(size_t)k * n + i] * a[(size_t)k * n + j];
+            a[(size_t)j * n + i] = v / d;
+        }
+    }
+    return 0;
+}
+
+static double host_normal(uint64_t seed, uint64_t stream, uint32_t purpose, uint32_t stage, uint64_t i, uint64_t d) {
+    const double pi = 2.0 * std::asin(1.0);
+    double r = smc::rng_uniform(seed, stream, purpose, stage, i, 2 * d);
+    double sv = smc::rng_uniform(seed, stream, purpose, stage, i, 2 * d + 1);
+    return std::sqrt(-2.0 * std::log(r)) * std::sin(2.0 * pi * sv);
+}
+
+static void write_stage_csv(const char *dir, int iter, const std::vector<double> &parts, const std::vector<double> &L,
+                            int N, int nd) {
+    // smc_fault.f90:923-936 / 1054-1067: ndim columns + likelihood, f20.5
+    std::string path = std::string(dir) + "/" + std::to_string(iter) + ".csv";
+    FILE *f = std::fopen(path.c_str(), "w");
+    if (!f) return;
+    for (int i = 0; i < N; ++i) {
+        for (int d = 0; d < nd; ++d) std::fprintf(f, "%20.5f", parts[(size_t)i * nd + d]);
+        std::fprintf(f, "%20.5f\n", L[i]);
+    }
+    std::fclose(f);
+}
+
+extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, int32_t N, uint64_t seed,
                                          const char *output_dir, double *particles_out, double *likelihood_out,
                                          double *evidence_out, int32_t *nstage_out) {
-    (void)range; (void)nparticle; (void)seed; (void)output_dir; (void)particles_out; (void)likelihood_out;
-    (void)evidence_out; (void)nstage_out;
     if (!ctx) return SMCGPU_ERR_ARG;
-    return ctx->fail(SMCGPU_ERR_STATE, "outer SMC not available in this build");
+    int r = check_ready(ctx);
+    if (r) return r;
+    if (!range || N < 2 || !evidence_out) return ctx->fail(SMCGPU_ERR_ARG, "fault_smc_exec: bad arguments");
+    CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+    if (output_dir) mkdir(output_dir, 0755);
+    const int nd = ctx->mesh.ndim_fault;
+    const uint64_t OS = smc::OUTER_STREAM;
+    cudaStream_t s = ctx->stream;
+    std::vector<double> parts((size_t)N * nd), Ls(N), w(N), mean(nd), cov((size_t)nd * nd);
+    std::vector<int32_t> assigned(N), sorted(N);
+    int status = 0;
+    smc::DevBuf<double> d_th, d_nl;
+    smc::DevBuf<int> d_st;
+    smc::DevBuf<unsigned long long> d_sid;
+    std::vector<int32_t> stv;
+    auto evaluate = [&](const std::vector<double> &th, const std::vector<unsigned long long> &sid,
+                        std::vector<double> &out) -> int {
+        int nb = (int)sid.size();
+        out.assign(nb, 0.0);
+        if (nb == 0) return SMCGPU_OK;
+        stv.assign(nb, 0);
+        CU(d_th.upload(th.data(), th.size(), s), "upload");
+        CU(d_sid.upload(sid.data(), sid.size(), s), "upload");
+        CU(d_nl.ensure(nb), "alloc");
+        CU(d_st.ensure(nb), "alloc");
+        int rr = nested_batch(ctx, nb, d_th.p, seed, d_sid.p, d_nl.p, d_st.p, NestedOpts());
+        if (rr) return rr;
+        CU(cudaMemcpyAsync(out.data(), d_nl.p, nb * sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
+        CU(cudaMemcpyAsync(stv.data(), d_st.p, nb * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+        CU(cudaStreamSynchronize(s), "sync");
+        for (int q = 0; q < nb; ++q) status |= stv[q];
+        return SMCGPU_OK;
+    };
+    // fault_sample_init_particles (smc_fault.f90:53-62)
+    for (int i = 0; i < N; ++i)
+        for (int d = 0; d < nd; ++d) {
+            double u = smc::rng_uniform(seed, OS, smc::RNG_OUT_INIT, 0, i, d);
+            parts[(size_t)i * nd + d] = range[2 * d] + u * (range[2 * d + 1] - range[2 * d]);
+        }
+    {
+        std::vector<unsigned long long> sid(N);
+        for (int i = 0; i < N; ++i) sid[i] = smc::eval_stream(0, 0, i);
+        r = evaluate(parts, sid, Ls);
+        if (r) return r;
+    }
+    if (output_dir) write_stage_csv(output_dir, 0, parts, Ls, N, nd);
+    double gamma = 0.0, evidence = 0.0;
+    int iter = 1;
+    CU(ctx->d_w.ensure(N), "alloc");
+    CU(ctx->d_counts.ensure(N), "alloc");
+    CU(ctx->d_flag.ensure(1), "alloc");
+    while (1.0 - gamma > std::pow(10.0, -8.0)) {
+        // fault_find_next_gamma (smc_fault.f90:392-485)
+        double gprev = gamma, minL = Ls[0];
+        for (int i = 0; i < N; ++i) minL = std::min(minL, Ls[i]);
+        double lower = gprev, upper = 1.0, err = 1.0, dg;
+        int cnt = 0;
+        while (err > std::pow(10.0, -8.0)) {
+            gamma = (lower + upper) / 2.0;
+            dg = gamma - gprev;
+            for (int i = 0; i < N; ++i) w[i] = std::exp(-dg * (Ls[i] - minL));
+            double m = 0.0;
+            for (int i = 0; i < N; ++i) m = m + w[i];
+            m = m / N;
+            double sd = 0.0;
+            for (int i = 0; i < N; ++i) sd = sd + (w[i] - m) * (w[i] - m);
+            sd = std::sqrt(sd / N);
+            double cv = sd / m;
+            if (cv > ctx->cfg.cv_outer) upper = gamma; else lower = gamma;
+            err = std::fabs(cv - ctx->cfg.cv_outer);
+            if (std::fabs(gamma - 1.0) < std::pow(10.0, -8.0)) break;
+            if (cnt > 1000) break;
+            cnt = cnt + 1;
+        }
+        double ev = 0.0;
+        dg = gamma - gprev;
+        for (int i = 0; i < N; ++i) ev = ev + std::exp(-dg * (Ls[i] - minL));
+        ev = ev / N;
+        evidence = evidence - std::log(ev) + dg * minL;
+        // fault_normalize_weights, fault_calc_mean_particles, fault_calc_cov_particles
+        double sum = 0.0;
+        for (int i = 0; i < N; ++i) sum = sum + w[i];
+        for (int i = 0; i < N; ++i) w[i] = w[i] / sum;
+        for (int d = 0; d < nd; ++d) mean[d] = 0.0;
+        for (int i = 0; i < N; ++i)
+            for (int d = 0; d < nd; ++d) mean[d] = mean[d] + w[i] * parts[(size_t)i * nd + d];
+        std::fill(cov.begin(), cov.end(), 0.0);
+        for (int i = 0; i < N; ++i) {
+            double wt = w[i];
+            for (int jd = 0; jd < nd; ++jd)
+                for (int id = jd; id < nd; ++id)
+                    cov[(size_t)jd * nd + id] = cov[(size_t)jd * nd + id] +
+                        wt * (parts[(size_t)i * nd + id] - mean[id]) * (parts[(size_t)i * nd + jd] - mean[jd]);
+        }
+        for (double &c : cov) c = c * 0.04;
+        if (chol_lower_inplace(cov, nd) != 0) status |= SMCGPU_ST_NONFINITE;
+        // fault_resample_particles on the device (bit-exact binary128 counts)
+        {
+            double uh, ul;
+            smc::rng_quad_uniform(seed, OS, smc::RNG_OUT_RES, iter, uh, ul);
+            CU(ctx->d_w.upload(w.data(), N, s), "upload");
+            CU(smc::launch_resample_counts(ctx->d_w.p, N, uh, ul, ctx->d_counts.p, ctx->d_flag.p, s), "resample");
+            CU(cudaMemcpyAsync(assigned.data(), ctx->d_counts.p, N * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+            CU(cudaStreamSynchronize(s), "sync");
+        }
+        // fault_reorder_to_send with qsort_ (one rank: the sorted order itself)
+        {
+            std::vector<int32_t> ta = assigned;
+            std::vector<double> tp = parts, tl = Ls;
+            for (int i = 0; i < N; ++i) sorted[i] = i + 1;
+            int32_t nn = N;
+            smcgpu_qsort_(assigned.data(), sorted.data(), &nn);
+            for (int k = 0; k < N; ++k) {
+                int org = sorted[k] - 1;
+                assigned[k] = ta[org];
+                for (int d = 0; d < nd; ++d) parts[(size_t)k * nd + d] = tp[(size_t)org * nd + d];
+                Ls[k] = tl[org];
+            }
+        }
+        // work_mcmc_sampling (smc_fault.f90:639-783): parents re-evaluated,
+        // then chained random-walk proposals, batched by chain position
+        std::vector<int32_t> start(N);
+        start[0] = 0;
+        for (int i = 0; i < N - 1; ++i) start[i + 1] = start[i] + assigned[i];
+        std::vector<double> curp = parts, Lcur, newp((size_t)N * nd), newL(N);
+        {
+            std::vector<unsigned long long> sid(N);
+            for (int i = 0; i < N; ++i) sid[i] = smc::eval_stream(iter, 0, i);
+            r = evaluate(parts, sid, Lcur);
+            if (r) return r;
+        }
+        int maxa = 0;
+        for (int i = 0; i < N; ++i) maxa = std::max(maxa, (int)assigned[i]);
+        for (int rr = 0; rr < maxa; ++rr) {
+            std::vector<int> who;
+            std::vector<double> cand;
+            std::vector<unsigned long long> sid;
+            for (int i = 0; i < N; ++i) {
+                if (assigned[i] <= rr) continue;
+                int j = start[i] + rr;
+                std::vector<double> z(nd), x(nd);
+                for (int d = 0; d < nd; ++d) z[d] = host_normal(seed, OS, smc::RNG_OUT_PROP, iter, j, d);
+                for (int jj = nd - 1; jj >= 0; --jj) {  // dtrmv('l','n','n')
+                    double t = z[jj];
+                    for (int ii = nd - 1; ii > jj; --ii) z[ii] += t * cov[(size_t)jj * nd + ii];
+                    z[jj] *= cov[(size_t)jj * nd + jj];
+                }
+                for (int d = 0; d < nd; ++d) x[d] = curp[(size_t)i * nd + d] + z[d];
+                for (int d = 0; d < nd; ++d) {
+                    double lo = range[2 * d], hi = range[2 * d + 1];
+                    if (hi - lo > 1e-3) {
+                        if (x[d] < lo) x[d] = std::min(2.0 * lo - x[d], hi);
+                        if (x[d] > hi) x[d] = std::max(2.0 * hi - x[d], lo);
+                    }
+                }
+                who.push_back(i);
+                cand.insert(cand.end(), x.begin(), x.end());
+                sid.push_back(smc::eval_stream(iter, 1, j));
+            }
+            std::vector<double> Lc;
+            r = evaluate(cand, sid, Lc);
+            if (r) return r;
+            for (size_t q = 0; q < who.size(); ++q) {
+                int i = who[q], j = start[i] + rr;
+                double mh = smc::rng_uniform(seed, OS, smc::RNG_OUT_MH, iter, j, 0);
+                if (gamma * (Lcur[i] - Lc[q]) > std::log(mh)) {
+                    for (int d = 0; d < nd; ++d) curp[(size_t)i * nd + d] = cand[q * nd + d];
+                    Lcur[i] = Lc[q];
+                }
+                newL[j] = Lcur[i];
+                for (int d = 0; d < nd; ++d) newp[(size_t)j * nd + d] = curp[(size_t)i * nd + d];
+            }
+        }
+        parts = newp;
+        Ls = newL;
+        if (output_dir) write_stage_csv(output_dir, iter, parts, Ls, N, nd);
+        iter = iter + 1;
+        if (iter > 100000) break;
+    }
+    if (particles_out) std::memcpy(particles_out, parts.data(), parts.size() * sizeof(double));
+    if (likelihood_out) std::memcpy(likelihood_out, Ls.data(), N * sizeof(double));
+    *evidence_out = evidence;
+    if (nstage_out) *nstage_out = iter - 1;
+    if (status) ctx->err = "fault_smc_exec: status bits " + std::to_string(status);
+    return SMCGPU_OK;
 }

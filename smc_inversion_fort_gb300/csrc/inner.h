@@ -1,0 +1,40 @@
+// Inner tempered SMC over slip (slip_smc_exec, smc_slip.f90:1445-1663):
+// per-batch argument block and launchers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.h"
+#include "mesh.h"
+
+namespace smc {
+
+struct InnerArgs {
+    int n_theta, N, NP2, D, mixed;
+    int ntau, tf, max_stages;
+    double cv, max_slip;
+    uint64_t seed;
+    const unsigned long long *streams;  // [n_theta]
+    // per-theta operator data
+    const double *A;      // [th][D][D] column-major Gram matrix
+    const double *b;      // [th][D]
+    const double *dsd;    // [th]
+    const double *lval;   // [th][nrow][9] values of L (columns in MeshDev::l_col)
+    const double *llval;  // [th][ll_nnz] values of L^T L on MeshDev::ll_ptr/ll_col
+    const ThetaAux *aux;  // [th]
+    // per-theta state (N = inner particles, NP2 = next power of two >= N)
+    double *parts, *parts_new;   // [th][N][D]
+    double *dbuf;                // [th][9][N]: L, P, Lnew, Pnew, w, dtau, dtau_new, score, spare
+    int *ibuf;                   // [th][4][NP2]: assigned, id_start, parent_of / queue keys, subset
+    // outputs
+    double *neglog;              // [th]
+    int *status;                 // [th]
+    int *nstage;                 // [th]
+    double *trace_gamma;         // optional [th][max_stages+2]
+    double *trace_inc;           // optional [th][max_stages+2]
+};
+
+cudaError_t launch_gibbs(const MeshDev &m, const InnerArgs &a, cudaStream_t s);
+cudaError_t launch_inner(const MeshDev &m, const InnerArgs &a, cudaStream_t s, const char **why);
+
+}  // namespace smc
