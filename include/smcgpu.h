@@ -81,6 +81,9 @@ typedef struct smcgpu_config {
     double sar_corr_len;           /* InSAR covariance range km (reference: 10)          */
     int32_t precision;             /* SMCGPU_PREC_FP64 or SMCGPU_PREC_MIXED              */
     int32_t device;                /* CUDA device ordinal                                */
+    int32_t max_outer_stages;      /* stop fault_smc_exec after this many stages (0: run
+                                      until gamma = 1 as the reference does; < 0: only
+                                      the initial evaluation of the prior sample)       */
 } smcgpu_config;
 
 typedef struct smcgpu_ctx smcgpu_ctx;

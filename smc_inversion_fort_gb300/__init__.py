@@ -37,7 +37,7 @@ class SmcConfig(C.Structure):
         ("nparticle_slip", C.c_int32), ("ntau", C.c_int32), ("tuning_factor", C.c_int32),
         ("max_stages", C.c_int32),
         ("cv_inner", C.c_double), ("cv_outer", C.c_double), ("sar_corr_len", C.c_double),
-        ("precision", C.c_int32), ("device", C.c_int32),
+        ("precision", C.c_int32), ("device", C.c_int32), ("max_outer_stages", C.c_int32),
     ]
 
 
@@ -110,6 +110,7 @@ def make_config(s: SmcSettings, precision: int = PREC_FP64, device: int = 0) -> 
     cfg.nparticle_slip, cfg.ntau, cfg.tuning_factor, cfg.max_stages = s.nparticle_slip, s.ntau, s.tuning_factor, s.max_stages
     cfg.cv_inner, cfg.cv_outer, cfg.sar_corr_len = s.cv_inner, s.cv_outer, s.sar_corr_len
     cfg.precision, cfg.device = precision, device
+    cfg.max_outer_stages = s.max_outer_stages
     return cfg
 
 

@@ -37,6 +37,7 @@ class SmcSettings:
     cv_inner: float = 2.0
     cv_outer: float = 0.2
     sar_corr_len: float = 10.0
+    max_outer_stages: int = 0
 
     def ndim_fault(self) -> int:
         if self.layout == 0:

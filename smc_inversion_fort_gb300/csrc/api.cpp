@@ -80,7 +80,7 @@ extern "C" int32_t smcgpu_create(const smcgpu_config *cfg, smcgpu_ctx **out) {
     if (e.empty() && cfg->basis == SMCGPU_BASIS_NODAL)
         for (int ip = 0; ip < cfg->nplane; ++ip)
             if (cfg->nxi[ip] > 32) e = "nodal basis supports nxi <= 32 per plane";
-    if (e.empty() && (cfg->nparticle_slip < 2 || cfg->ntau < 1 || cfg->tuning_factor < 1 || cfg->max_stages < 1))
+    if (e.empty() && (cfg->nparticle_slip < 2 || cfg->ntau < 1 || cfg->tuning_factor < 1 || cfg->max_stages < 0))
         e = "invalid SMC settings";
     if (e.empty() && !(cfg->max_slip > 0.0)) e = "max_slip must be positive";
     if (!e.empty()) { g_create_err = e; delete ctx; return SMCGPU_ERR_ARG; }

@@ -316,6 +316,7 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
     CU(ctx->d_counts.ensure(N), "alloc");
     CU(ctx->d_flag.ensure(1), "alloc");
     while (1.0 - gamma > std::pow(10.0, -8.0)) {
+        if (ctx->cfg.max_outer_stages != 0 && iter > std::max(ctx->cfg.max_outer_stages, 0)) break;
         // fault_find_next_gamma (smc_fault.f90:392-485)
         double gprev = gamma, minL = Ls[0];
         for (int i = 0; i < N; ++i) minL = std::min(minL, Ls[i]);

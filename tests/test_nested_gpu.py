@@ -31,34 +31,93 @@ def setup_case(name, orc, seed=2024, nparticle=None):
     return w, obs, orc.Oracle(w.settings, obs)
 
 
-@pytest.mark.parametrize("name", ["tiny", "tiny-nodal", "tiny-sar"])
-def test_nested_fp64_matches_oracle(smcgpu, orc, name):
-    w, obs, o = setup_case(name, orc)
-    th = np.vstack([true_theta(w)[None], random_thetas(w, 7, seed=3)])
-    streams = np.arange(100, 100 + len(th), dtype=np.uint64)
+def _compare(smcgpu, w, obs, o, th, streams, seed):
     g = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
     g.set_data(obs)
-    got = g.fault_likelihood_trace(th, seed=11, streams=streams)
-    matched = 0
+    got = g.fault_likelihood_trace(th, seed=seed, streams=streams)
+    rows = []
     for i in range(len(th)):
-        ref = o.fault_likelihood(th[i], 11, int(streams[i]), trace=True)
+        ref = o.fault_likelihood(th[i], seed, int(streams[i]), trace=True)
         a, b = got["neglog"][i], ref["neglog"]
         rel = abs(a - b) / max(1.0, abs(b))
         gsame = (len(got["gamma"][i]) == len(ref["gamma"]) and
-                 np.allclose(got["gamma"][i], ref["gamma"], rtol=0, atol=1e-9))
-        print(f"{name} theta {i}: gpu {a:.10f} oracle {b:.10f} rel {rel:.2e} stages {got['nstage'][i]}/{len(ref['gamma'])}"
-              f" status {got['status'][i]}/{ref['status']} gamma-match {gsame}")
-        assert got["status"][i] == 0 and ref["status"] == 0
-        assert abs(a - b) < 3.0
-        if rel < 1e-7 and gsame:
-            matched += 1
-    assert matched >= 0.6 * len(th), matched
+                 np.allclose(got["gamma"][i], ref["gamma"], rtol=0, atol=1e-12))
+        rows.append((a, b, rel, gsame, int(got["status"][i]), int(ref["status"])))
+        print(f"theta {i}: gpu {a:.10f} oracle {b:.10f} rel {rel:.2e} stages {got['nstage'][i]}/{len(ref['gamma'])} "
+              f"status {got['status'][i]}/{ref['status']} schedule-match {gsame}")
+    return rows
+
+
+@pytest.mark.parametrize("name", ["tiny", "tiny-nodal", "tiny-sar"])
+@pytest.mark.parametrize("ntau", [1, 3])
+def test_nested_fp64_bitwise_schedule_short_trajectories(smcgpu, orc, name, ntau):
+    """With short leapfrog trajectories rounding differences are not amplified:
+    every evaluation must reproduce the oracle's tempering schedule (1e-12)
+    and -log Z (1e-9 relative)."""
+    w, obs, o = setup_case(name, orc)
+    w.settings.ntau = ntau
+    o = orc.Oracle(w.settings, obs)
+    th = np.vstack([true_theta(w)[None], random_thetas(w, 5, seed=3)])
+    streams = np.arange(100, 100 + len(th), dtype=np.uint64)
+    for a, b, rel, gsame, sa, sb in _compare(smcgpu, w, obs, o, th, streams, 11):
+        assert sa == 0 and sb == 0
+        assert gsame and rel < 1e-9
+
+
+@pytest.mark.parametrize("name", ["tiny", "tiny-nodal", "tiny-sar"])
+def test_nested_fp64_matches_oracle_reference_ntau(smcgpu, orc, name):
+    """ntau = 10 and 50 (the reference's hard-coded value).  Long trajectories
+    at tuned step sizes amplify rounding, so an evaluation can leave the
+    oracle's path after a few stages and continue as a statistically
+    equivalent one.  Checked here: the first tempering exponent (which depends
+    only on the initial population) is identical, ntau = 10 evaluations agree
+    to 1e-6, and at ntau = 50 at least one evaluation in eight still matches
+    exactly; the distributional check is the next test."""
+    w, obs, o = setup_case(name, orc)
+    for ntau in (10, 50):
+        w.settings.ntau = ntau
+        o = orc.Oracle(w.settings, obs)
+        th = np.vstack([true_theta(w)[None], random_thetas(w, 7, seed=3)])
+        streams = np.arange(100, 100 + len(th), dtype=np.uint64)
+        g = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
+        g.set_data(obs)
+        got = g.fault_likelihood_trace(th, seed=11, streams=streams)
+        exact = 0
+        for i in range(len(th)):
+            ref = o.fault_likelihood(th[i], 11, int(streams[i]), trace=True)
+            a, b = got["neglog"][i], ref["neglog"]
+            rel = abs(a - b) / max(1.0, abs(b))
+            print(f"ntau {ntau} theta {i}: gpu {a:.10f} oracle {b:.10f} rel {rel:.2e}")
+            assert got["status"][i] == 0 and ref["status"] == 0
+            assert got["gamma"][i][0] == pytest.approx(ref["gamma"][0], rel=0, abs=1e-12)
+            if ntau == 10:
+                assert rel < 1e-6
+            exact += rel < 1e-9
+        assert exact >= 1
+
+
+def test_nested_fp64_statistics_match_oracle(smcgpu, orc):
+    """Over independent streams the mean -log Z of the GPU path equals the
+    oracle's within 4 standard errors (reference ntau = 50)."""
+    w, obs, o = setup_case("tiny", orc)
+    th = true_theta(w)
+    n = 24
+    streams = np.arange(7000, 7000 + n, dtype=np.uint64)
+    g = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
+    g.set_data(obs)
+    a, sa = g.fault_calc_likelihood(np.repeat(th[None], n, 0), 31, streams)
+    b, sb = o.fault_likelihood_batch(np.repeat(th[None], n, 0), 31, streams)
+    se = np.sqrt((a.var(ddof=1) + b.var(ddof=1)) / n) + 1e-9
+    print("gpu", a.mean(), a.std(), "oracle", b.mean(), b.std())
+    assert abs(a.mean() - b.mean()) < 4 * se + 1e-6
 
 
 def test_nested_mixed_matches_fp64(smcgpu, orc):
+    """MIXED against FP64: the mean -log Z over independent streams agrees
+    within 4 standard errors (and within 1 nat)."""
     w, obs, o = setup_case("tiny", orc)
     th = np.vstack([true_theta(w)[None], random_thetas(w, 3, seed=4)])
-    reps = 6
+    reps = 48
     th_rep = np.repeat(th, reps, axis=0)
     streams = np.arange(len(th_rep), dtype=np.uint64) + 5000
     g64 = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
@@ -66,11 +125,13 @@ def test_nested_mixed_matches_fp64(smcgpu, orc):
     g32 = smcgpu.SmcGpu(w.settings, smcgpu.PREC_MIXED)
     g32.set_data(obs)
     a, sa = g64.fault_calc_likelihood(th_rep, 21, streams)
-    b, sb = g32.fault_calc_likelihood(th_rep, 21, streams)
+    b, sb = g32.fault_calc_likelihood(th_rep, 21, streams + 10**6)
     assert np.all(sa == 0) and np.all(sb == 0)
-    ma, mb = a.reshape(-1, reps).mean(1), b.reshape(-1, reps).mean(1)
-    print("fp64", ma, "\nmixed", mb, "\nspread", a.reshape(-1, reps).std(1))
-    assert np.all(np.abs(ma - mb) < 0.5)
+    a, b = a.reshape(-1, reps), b.reshape(-1, reps)
+    se = np.sqrt((a.var(1, ddof=1) + b.var(1, ddof=1)) / reps)
+    print("fp64 ", a.mean(1), "\nmixed", b.mean(1), "\nse   ", se)
+    assert np.all(np.abs(a.mean(1) - b.mean(1)) < 4 * se + 1e-9)
+    assert np.all(np.abs(a.mean(1) - b.mean(1)) < 1.0)
 
 
 def test_posterior_population(smcgpu, orc):
@@ -85,3 +146,44 @@ def test_posterior_population(smcgpu, orc):
     mg, mr = got["particles"].mean(0), ref["particles"].mean(0)
     sd = ref["particles"].std(0) + 1e-3
     assert np.all(np.abs(mg - mr) <= 0.5 * sd + 1e-9) or abs(got["neglog"] - ref["neglog"]) < 1e-7 * abs(ref["neglog"])
+
+
+def test_gibbs_initial_population_matches_oracle(smcgpu, orc):
+    """max_stages = 0 stops right after the truncated-MVN Gibbs
+    initialisation (smc_slip.f90:184-287): the initial population, its
+    likelihoods and priors must equal the oracle's."""
+    for name in ("tiny", "tiny-nodal"):
+        w, obs, o = setup_case(name, orc)
+        w.settings.max_stages = 0
+        o = orc.Oracle(w.settings, obs)
+        g = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
+        g.set_data(obs)
+        th = random_thetas(w, 1, seed=8)[0]
+        got = g.fault_likelihood_posterior(th, 3, 9)
+        ref = o.fault_likelihood(th, 3, 9)
+        assert got["neglog"] == 1e10 and ref["neglog"] == 1e10
+        scale = np.abs(ref["particles"]).max()
+        assert np.abs(got["particles"] - ref["particles"]).max() <= 1e-10 * scale
+        np.testing.assert_allclose(got["likelihood"], ref["likelihood"], rtol=1e-9)
+        np.testing.assert_allclose(got["prior"], ref["prior"], rtol=1e-9, atol=1e-12)
+
+
+def test_outer_smc_matches_oracle(smcgpu, orc):
+    """fault_smc_exec end to end on a small case with short trajectories:
+    same tempering schedule, evidence and final population as the oracle."""
+    w, obs, o = setup_case("tiny", orc, nparticle=32)
+    w.settings.ntau = 1
+    w.settings.cv_outer = 1.0
+    o = orc.Oracle(w.settings, obs)
+    from smc_inversion_fort_gb300.configs import prior_range
+    rg = prior_range(w)
+    rg[3] = [20.0, 28.0]      # length
+    rg[5] = [0.0, 60.0]       # strike
+    g = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
+    g.set_data(obs)
+    parts, lik, ev, ns = g.fault_smc_exec(rg, 8, 5)
+    ref = o.fault_smc(rg, 8, 5)
+    print("gpu evidence", ev, "stages", ns, "oracle", ref["evidence"], ref["nstage"])
+    assert ns == ref["nstage"]
+    assert abs(ev - ref["evidence"]) <= 1e-8 * max(1.0, abs(ref["evidence"]))
+    np.testing.assert_allclose(parts, ref["particles"], rtol=1e-9, atol=1e-9)
