@@ -125,6 +125,19 @@ int32_t smcgpu_greens_batch(smcgpu_ctx *ctx, int32_t n_theta, const double *thet
 int32_t smcgpu_greens_batch_dev(smcgpu_ctx *ctx, int32_t n_theta, const double *theta_dev,
                                 int32_t precision, void *gmat_dev);
 
+/* smcgpu_greens_batch_dev for callers that cannot allocate device memory
+ * during the call: hosts that give the whole GPU memory to their own pool
+ * at start-up, and stage loops that must not pay cudaMalloc/cudaFree's
+ * device-wide synchronisation.  It has no counterpart in the reference.  Its
+ * scratch (per-plane geometry records) is a fixed device array of 16384
+ * records (2.2 MB on every GPU that loads the library), so n_theta * nplane
+ * must be <= 16384, otherwise SMCGPU_ERR_ARG.  No cudaMalloc, cudaFree or
+ * allocating library call is made.  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) and should come before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
+int32_t smcgpu_greens_batch_noalloc(smcgpu_ctx *ctx, int32_t n_theta, const double *theta_dev,
+                                    int32_t precision, void *gmat_dev);
+
 /* Nested evaluation -log Z(theta) for n_theta geometries (fault_calc_likelihood,
  * smc_fault.f90:66-292).  Every evaluation draws from the Philox4x64-10 stream
  * keyed by (seed, streams[i]); status_out gets SMCGPU_ST_* bits; a stage-cap
