@@ -40,6 +40,8 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n-theta", type=int, default=8192)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-nested", action="store_true")
+    p.add_argument("--outer-stages", type=int, default=1)
     return p.parse_args()
 
 
@@ -164,6 +166,85 @@ def load_traffic():
         with open(p) as f:
             return json.load(f)
     return None
+
+
+def nested_workload(seed=2024):
+    """c0: 8x4 patches x 2 components (D = 64), 60 three-component GNSS
+    stations, 500 inner and 500 outer particles; data from the known fault."""
+    from smc_inversion_fort_gb300.configs import make_stations, preset, prior_range, true_slip, true_theta
+    w = preset("c0")
+    rng = np.random.default_rng(seed)
+    obs = make_stations(w, rng)
+    return w, obs, rng, prior_range(w), true_theta(w), true_slip(w)
+
+
+def nested_bench(pkg, torch, stages=1, cpu=True):
+    """Outer particles/s of the nested SMC on c0, FP64 and MIXED, and the
+    MIXED-vs-FP64 evidence difference."""
+    import dataclasses
+    w, obs, rng, rg, th_true, s_true = nested_workload()
+    obs["dvec"] = np.zeros(len(obs["obs_sigma"]))
+    g = pkg.SmcGpu(w.settings)
+    g.set_data(obs)
+    G = g.calc_greens_func(th_true[None])[0]
+    obs["dvec"] = G.T @ s_true + rng.standard_normal(G.shape[1]) * obs["obs_sigma"]
+    out = {"workload": "c0: 8x4 patches (D=64), 60 GNSS stations (180 obs), 500 inner x 500 outer particles, "
+                       "ntau 50, CV 2 / 0.2", "n_outer": w.n_outer, "timed_outer_stages": stages}
+    for name, prec in (("mixed", pkg.PREC_MIXED), ("fp64", pkg.PREC_FP64)):
+        times = {}
+        for k in (-1, stages):
+            s2 = dataclasses.replace(w.settings, max_outer_stages=k)
+            gg = pkg.SmcGpu(s2, prec)
+            gg.set_data(obs)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _, _, ev, ns = gg.fault_smc_exec(rg, w.n_outer, 17)
+            torch.cuda.synchronize()
+            times[k] = time.perf_counter() - t0
+            gg.close()
+        per_stage = (times[stages] - times[-1]) / stages
+        out[name] = {"outer_particles_per_s": w.n_outer / per_stage, "s_per_outer_stage": per_stage,
+                     "nested_evals_per_s": 2 * w.n_outer / per_stage, "init_eval_s": times[-1]}
+    # evidence agreement on the true geometry over independent streams
+    reps = 64
+    thr = np.repeat(th_true[None], reps, 0)
+    st = np.arange(reps, dtype=np.uint64)
+    res = {}
+    for name, prec in (("mixed", pkg.PREC_MIXED), ("fp64", pkg.PREC_FP64)):
+        gg = pkg.SmcGpu(w.settings, prec)
+        gg.set_data(obs)
+        res[name], _ = gg.fault_calc_likelihood(thr, 99, st + (0 if name == "fp64" else 10**6))
+        gg.close()
+    d = res["mixed"].mean() - res["fp64"].mean()
+    se = float(np.sqrt((res["mixed"].var(ddof=1) + res["fp64"].var(ddof=1)) / reps))
+    out["mixed_vs_fp64"] = {"delta_neglog_evidence": float(d), "standard_error": se, "reps": reps,
+                            "fp64_mean": float(res["fp64"].mean()), "fp64_std": float(res["fp64"].std())}
+    out["mixed_speedup_vs_fp64"] = out["mixed"]["outer_particles_per_s"] / out["fp64"]["outer_particles_per_s"]
+    if cpu:
+        out["cpu_baseline"] = cpu_nested_rate(w, obs, rg)
+        out["mixed_speedup_vs_cpu"] = out["mixed"]["outer_particles_per_s"] / out["cpu_baseline"]["value"]
+    return out
+
+
+def cpu_nested_rate(w, obs, rg, target_s=15.0):
+    """Oracle nested evaluations of prior-box geometries on all host threads
+    (one geometry per thread, as the reference's MPI ranks); outer particles
+    per second = evaluations per second / 2."""
+    from oracle import pyoracle
+    pyoracle.build()
+    o = pyoracle.Oracle(w.settings, obs)
+    nthreads = os.cpu_count() or 1
+    rng = np.random.default_rng(5)
+    th = rg[:, 0] + rng.uniform(0, 1, (4 * nthreads, len(rg))) * (rg[:, 1] - rg[:, 0])
+    t0 = time.perf_counter()
+    o.fault_likelihood_batch(th[:nthreads], 1, np.arange(nthreads, dtype=np.uint64), nthreads=nthreads)
+    t1 = time.perf_counter() - t0
+    n = int(min(len(th), max(nthreads, nthreads * round(target_s / max(t1, 1e-3)))))
+    t0 = time.perf_counter()
+    o.fault_likelihood_batch(th[:n], 1, np.arange(n, dtype=np.uint64), nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt / 2.0, "unit": "outer particles/s", "cores": nthreads, "kind": "port",
+            "sample": f"{n} nested evaluations of prior-box geometries, {dt:.1f} s wall"}
 
 
 def gb300_arm(args):
@@ -296,6 +377,12 @@ def gb300_arm(args):
         line["roofline"]["traffic_source"] = tr.get("source")
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_greens_rate(w, obs, th)
+    if not args.no_nested:
+        g.close()
+        del out, dth
+        torch.cuda.empty_cache()
+        line["nested_smc"] = nested_bench(pkg, torch, stages=args.outer_stages,
+                                          cpu=(rank == 0 and not args.no_cpu_baseline))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -1396,6 +1396,7 @@ extern "C" int orc_fault_smc(const orc_setup *s, const double *range, int32_t N,
     double gamma = 0.0, evidence = 0.0;
     int iter = 1;
     while (1.0 - gamma > pow(10.0, -8.0)) {
+        if (s->max_outer_stages != 0 && iter > std::max(s->max_outer_stages, 0)) break;
         // fault_find_next_gamma (:392-485)
         double gprev = gamma, minL = Ls[0];
         for (int i = 0; i < N; ++i) minL = std::min(minL, Ls[i]);

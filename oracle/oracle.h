@@ -53,6 +53,7 @@ typedef struct orc_setup {
     const double *obs_sigma;     /* [nobs] cm */
     const double *dvec;          /* [nobs] cm */
     const double *sigma_sar_inv; /* concatenated per path, nsar_p x nsar_p column-major */
+    int32_t max_outer_stages;    /* 0: until gamma = 1; < 0: initial evaluation only; k: k stages */
 } orc_setup;
 
 typedef struct orc_dims_t {

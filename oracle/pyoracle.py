@@ -36,6 +36,7 @@ class OrcSetup(C.Structure):
         ("nobs", C.c_int32), ("nsar_total", C.c_int32), ("ngnss", C.c_int32), ("npath", C.c_int32),
         ("nsar_index", C.c_void_p), ("obs_points", C.c_void_p), ("obs_unitvec", C.c_void_p),
         ("obs_sigma", C.c_void_p), ("dvec", C.c_void_p), ("sigma_sar_inv", C.c_void_p),
+        ("max_outer_stages", C.c_int32),
     ]
 
 
@@ -128,6 +129,7 @@ class Oracle:
         st.nobs, st.nsar_total, st.ngnss, st.npath = nobs, nsar, self.ngnss, self.npath
         st.nsar_index, st.obs_points, st.obs_unitvec = _p(self.idx0), _p(self.pts), _p(self.e)
         st.obs_sigma, st.dvec, st.sigma_sar_inv = _p(self.sig), _p(self.d), _p(self.sinv)
+        st.max_outer_stages = getattr(s, "max_outer_stages", 0)
         self.st = st
         dm = OrcDims()
         lib().orc_dims(C.byref(st), C.byref(dm))

@@ -18,8 +18,10 @@ LIBDIR = os.path.join(PKG, "_lib")
 OBJDIR = os.path.join(PKG, "_build")
 LIB = os.path.join(LIBDIR, "libsmcgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no FMA contraction, so the host-side stage arithmetic of the
+# outer SMC rounds like the reference's (and the oracle's) on every CPU
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-              "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
+              "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
 
 
 def _nvcc() -> str:

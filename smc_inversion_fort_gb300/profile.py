@@ -1,0 +1,69 @@
+"""Fixed small workloads for profiling one kernel family at a time.
+
+    python -m smc_inversion_fort_gb300.profile greens [--n-theta 256] [--fp32] [--reps 2]
+    python -m smc_inversion_fort_gb300.profile nested [--n-theta 16] [--mixed] [--reps 1]
+
+`greens` runs the Green's build of the 16x8-patch, 5x5-Gauss-point,
+400-station workload on n geometries; `nested` runs nested evaluations of the
+8x4-patch, 60-station, 500-particle workload.  Each rep is one batch.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+import numpy as np
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("what", choices=["greens", "nested"])
+    p.add_argument("--n-theta", type=int, default=0)
+    p.add_argument("--fp32", action="store_true")
+    p.add_argument("--mixed", action="store_true")
+    p.add_argument("--reps", type=int, default=2)
+    a = p.parse_args(argv)
+    import torch
+
+    import smc_inversion_fort_gb300 as pkg
+    from smc_inversion_fort_gb300.configs import make_stations, preset, random_thetas, true_slip, true_theta
+
+    if a.what == "greens":
+        w = preset("c1")
+        n = a.n_theta or 256
+        obs = make_stations(w, np.random.default_rng(2024))
+        obs["dvec"] = np.zeros(len(obs["obs_sigma"]))
+        g = pkg.SmcGpu(w.settings)
+        g.set_data(obs)
+        dm = g.dims()
+        th = torch.from_numpy(random_thetas(w, n, seed=7)).cuda()
+        prec = pkg.PREC_FP32 if a.fp32 else pkg.PREC_FP64
+        out = torch.empty((n, dm["D"], dm["nobs"]), dtype=torch.float32 if a.fp32 else torch.float64, device="cuda")
+        for _ in range(a.reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            g.greens_dev(n, th.data_ptr(), out.data_ptr(), prec)
+            torch.cuda.synchronize()
+            print(f"greens n_theta={n} {'fp32' if a.fp32 else 'fp64'}: {1e3 * (time.perf_counter() - t0):.2f} ms")
+    else:
+        w = preset("c0")
+        n = a.n_theta or 16
+        rng = np.random.default_rng(2024)
+        obs = make_stations(w, rng)
+        obs["dvec"] = np.zeros(len(obs["obs_sigma"]))
+        prec = pkg.PREC_MIXED if a.mixed else pkg.PREC_FP64
+        g = pkg.SmcGpu(w.settings, prec)
+        g.set_data(obs)
+        G = g.calc_greens_func(true_theta(w)[None])[0]
+        obs["dvec"] = G.T @ true_slip(w) + rng.standard_normal(G.shape[1]) * obs["obs_sigma"]
+        g.set_data(obs)
+        th = np.vstack([true_theta(w)[None], random_thetas(w, n - 1, seed=3)])
+        for r in range(a.reps):
+            t0 = time.perf_counter()
+            nl, st = g.fault_calc_likelihood(th, 1, np.arange(n, dtype=np.uint64) + 1000 * r)
+            print(f"nested n_theta={n} {'mixed' if a.mixed else 'fp64'}: {time.perf_counter() - t0:.3f} s, "
+                  f"-logZ[0] {nl[0]:.4f}, status {int(st.max())}")
+
+
+if __name__ == "__main__":
+    main()
