@@ -3,6 +3,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -36,7 +37,7 @@ int next_pow2(int n) {
 size_t bytes_per_theta(const smcgpu_ctx *ctx) {
     const smc::MeshPattern &p = ctx->mesh;
     size_t D = p.D, N = ctx->cfg.nparticle_slip, NP2 = next_pow2((int)N);
-    size_t b = D * ctx->nobs * 8 + D * std::max(ctx->nsar, 0) * 8 + D * D * 8 + D * 8 + 8;
+    size_t b = D * ctx->nobs * 8 + D * std::max(ctx->nsar, 0) * 8 + D * D * 12 + D * 8 + 8;
     b += (size_t)p.nrow * 9 * 8 + D * 9 * 8 + p.ll_col.size() * 8 + sizeof(smc::ThetaAux);
     b += 2 * N * D * 8 + 9 * N * 8 + 4 * NP2 * 4 + p.nplane * sizeof(smc::PlaneGeom) + 64;
     return b;
@@ -67,6 +68,7 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
     CU(ctx->d_parts_new.ensure((size_t)chunk * N * D), "alloc particles");
     CU(ctx->d_dbuf.ensure((size_t)chunk * 9 * N), "alloc dbuf");
     CU(ctx->d_ibuf.ensure((size_t)chunk * 4 * NP2), "alloc ibuf");
+    CU(ctx->d_A32.ensure((size_t)chunk * D * D), "alloc A32");
     CU(ctx->d_nstage_tmp.ensure((size_t)chunk), "alloc");
     for (int t0 = 0; t0 < n; t0 += chunk) {
         int nb = std::min(chunk, n - t0);
@@ -94,7 +96,9 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
         a.trace_inc = opt.trace_inc ? opt.trace_inc + (size_t)t0 * (a.max_stages + 2) : nullptr;
         CU(smc::launch_gibbs(ctx->md, a, s), "gibbs kernel");
         const char *why = nullptr;
-        cudaError_t e = smc::launch_inner(ctx->md, a, s, &why);
+        a.A32 = ctx->d_A32.p;
+        static const bool use_cta = getenv("SMCGPU_INNER_CTA") != nullptr;
+        cudaError_t e = use_cta ? smc::launch_inner(ctx->md, a, s, &why) : smc::launch_inner_warp(ctx->md, a, s, &why);
         if (e != cudaSuccess) {
             if (why) return ctx->fail(SMCGPU_ERR_ARG, why);
             return ctx->cuda_fail(e, "inner kernel");
@@ -389,19 +393,28 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
         std::vector<int32_t> start(N);
         start[0] = 0;
         for (int i = 0; i < N - 1; ++i) start[i + 1] = start[i] + assigned[i];
-        std::vector<double> curp = parts, Lcur, newp((size_t)N * nd), newL(N);
-        {
-            std::vector<unsigned long long> sid(N);
-            for (int i = 0; i < N; ++i) sid[i] = smc::eval_stream(iter, 0, i);
-            r = evaluate(parts, sid, Lcur);
-            if (r) return r;
-        }
+        std::vector<double> curp = parts, Lcur(N), newp((size_t)N * nd), newL(N);
         int maxa = 0;
         for (int i = 0; i < N; ++i) maxa = std::max(maxa, (int)assigned[i]);
-        for (int rr = 0; rr < maxa; ++rr) {
+        for (int rr = 0; rr < std::max(maxa, 1); ++rr) {
             std::vector<int> who;
             std::vector<double> cand;
             std::vector<unsigned long long> sid;
+            std::vector<int> pidx;
+            if (rr == 0) {
+                // the parents' re-evaluation (smc_fault.f90:695-707) does not
+                // depend on any Metropolis decision, so it shares the first
+                // round's batch: parents first, then their first proposals.
+                // Parents without children are skipped: their value is never
+                // used (the reference computes and discards it).
+                for (int i = 0; i < N; ++i) {
+                    if (assigned[i] == 0) continue;
+                    pidx.push_back(i);
+                    cand.insert(cand.end(), parts.begin() + (size_t)i * nd, parts.begin() + (size_t)(i + 1) * nd);
+                    sid.push_back(smc::eval_stream(iter, 0, i));
+                }
+            }
+            const size_t npar = sid.size();
             for (int i = 0; i < N; ++i) {
                 if (assigned[i] <= rr) continue;
                 int j = start[i] + rr;
@@ -424,15 +437,17 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
                 cand.insert(cand.end(), x.begin(), x.end());
                 sid.push_back(smc::eval_stream(iter, 1, j));
             }
-            std::vector<double> Lc;
-            r = evaluate(cand, sid, Lc);
+            std::vector<double> Lall;
+            r = evaluate(cand, sid, Lall);
             if (r) return r;
+            for (size_t q = 0; q < npar; ++q) Lcur[pidx[q]] = Lall[q];
             for (size_t q = 0; q < who.size(); ++q) {
                 int i = who[q], j = start[i] + rr;
+                double Lq = Lall[npar + q];
                 double mh = smc::rng_uniform(seed, OS, smc::RNG_OUT_MH, iter, j, 0);
-                if (gamma * (Lcur[i] - Lc[q]) > std::log(mh)) {
-                    for (int d = 0; d < nd; ++d) curp[(size_t)i * nd + d] = cand[q * nd + d];
-                    Lcur[i] = Lc[q];
+                if (gamma * (Lcur[i] - Lq) > std::log(mh)) {
+                    for (int d = 0; d < nd; ++d) curp[(size_t)i * nd + d] = cand[(npar + q) * nd + d];
+                    Lcur[i] = Lq;
                 }
                 newL[j] = Lcur[i];
                 for (int d = 0; d < nd; ++d) newp[(size_t)j * nd + d] = curp[(size_t)i * nd + d];

@@ -193,20 +193,34 @@ __global__ void gibbs_kernel(MeshDev m, InnerArgs a) {
     __syncwarp();
     const double pi = 3.141592653589793;
     for (int k = 0; k < N; ++k) {
-        for (int d = lane; d < D; d += 32) vn[d] = rng_normal(a.seed, stream, RNG_GIBBS, 0, k, d);
+        for (int d = lane; d < D; d += 32)
+            vn[d] = MIXED ? (double)rng_normal_f(a.seed, stream, RNG_GIBBS, 0, k, d)
+                          : rng_normal(a.seed, stream, RNG_GIBBS, 0, k, d);
         __syncwarp();
         for (int i = 0; i < D; ++i) {
             int e0 = m.ll_ptr[i], e1 = m.ll_ptr[i + 1];
             // diagonal entry and the conditional mean
-            double lii = 0.0, term = 0.0;
             int e = e0 + lane;
             int j = e < e1 ? m.ll_col[e] : -1;
             double v = e < e1 ? ll[e] : 0.0;
-            if (j == i) lii = v;
-            lii = warp_sum(lii);
-            double s2 = 1.0 / (lii / alpha2);
-            if (j >= 0 && j != i) term = v / alpha2 * cur[j] * s2;
-            double mu = -warp_sum(term);
+            double s2, mu;
+            if (!MIXED) {
+                double lii = (j == i) ? v : 0.0, term = 0.0;
+                lii = warp_sum(lii);
+                s2 = 1.0 / (lii / alpha2);
+                if (j >= 0 && j != i) term = v / alpha2 * cur[j] * s2;
+                mu = -warp_sum(term);
+            } else {
+                float lii = (j == i) ? (float)v : 0.0f, term = 0.0f;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) lii += __shfl_xor_sync(0xffffffffu, lii, o);
+                if (j >= 0 && j != i) term = (float)v * (float)cur[j];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+                float s2f = (float)alpha2 / lii;
+                s2 = (double)s2f;
+                mu = (double)(-term / lii);
+            }
             if (lane == 0) {
                 double v1 = vn[i];
                 double y;
@@ -310,7 +324,10 @@ __global__ void __launch_bounds__(NT, 1) inner_kernel(MeshDev m, InnerArgs a) {
     T *Asm = Msm + DP * DP;                      // DP*DP
     T *Xb0 = Asm + DP * DP;                      // DP*C
     T *Xb1 = Xb0 + DP * C;
-    double *vb = (double *)(Xb1 + DP * C);       // b
+    // per-row constants of the stage in the leapfrog's own precision, so the
+    // step loop never touches the FP64 pipe in MIXED mode
+    T *tcov = Xb1 + DP * C, *tmean = tcov + DP, *tcv = tmean + DP, *tisc = tcv + DP;
+    double *vb = (double *)(tisc + DP);          // b
     double *vcov = vb + DP, *vmean = vcov + DP, *vg = vmean + DP, *vh = vg + DP, *vc = vh + DP;
     double *red = vc + DP;                       // TYN*C
     double *scr = red + TYN * C;                 // 64 doubles (also 32 dd)
@@ -533,6 +550,12 @@ __global__ void __launch_bounds__(NT, 1) inner_kernel(MeshDev m, InnerArgs a) {
                 s_Pbar = pr;
             }
         }
+        for (int i = tid; i < DP; i += NT) {
+            tcov[i] = (T)vcov[i];
+            tmean[i] = (T)vmean[i];
+            tcv[i] = MIXED ? (T)vc[i] : (T)(gamma * vb[i]);
+            tisc[i] = (T)(1.0 / sqrt(vcov[i]));
+        }
         __syncthreads();
 
         // ---- one HMC pass: tuning (every tf-th parent) or sampling
@@ -627,13 +650,17 @@ __global__ void __launch_bounds__(NT, 1) inner_kernel(MeshDev m, InnerArgs a) {
                         if (s.fresh[c]) xc[i][q] = (act && r < D) ? (T)parts[(size_t)s.par[c] * D + r] : T(0);
                         T pv = T(0);
                         if (act && r < D) {
-                            if (MIXED) pv = (T)(rng_normal_f(a.seed, stream, P_MOM, iter, s.j[c], r) / sqrt(vcov[r]));
-                            else pv = (T)(rng_normal(a.seed, stream, P_MOM, iter, s.j[c], r) / sqrt(vcov[r]));
-                            kin[q] += (double)pv * vcov[r] * (double)pv / 2.0;
+                            if (MIXED) {
+                                pv = rng_normal_f(a.seed, stream, P_MOM, iter, s.j[c], r) * tisc[r];
+                                kin[q] += (double)(pv * tcov[r] * pv * T(0.5));
+                            } else {
+                                pv = (T)(rng_normal(a.seed, stream, P_MOM, iter, s.j[c], r) / sqrt(vcov[r]));
+                                kin[q] += (double)pv * vcov[r] * (double)pv / 2.0;
+                            }
                         }
                         p[i][q] = pv;
                         x[i][q] = xc[i][q];
-                        T xv = MIXED ? (T)((double)x[i][q] - vmean[r < DP ? r : 0]) : x[i][q];
+                        T xv = MIXED ? x[i][q] - tmean[r] : x[i][q];
                         Xb0[(size_t)r * C + c] = (r < D) ? xv : T(0);
                     }
                     red[ty * C + c] = kin[q];
@@ -662,7 +689,7 @@ __global__ void __launch_bounds__(NT, 1) inner_kernel(MeshDev m, InnerArgs a) {
                         for (int i = 0; i < RT; ++i) {
                             int r = ty * RT + i;
                             if (!live || r >= D) continue;
-                            T gr = MIXED ? (T)vc[r] + acc[i][q] : acc[i][q] - (T)(gamma * vb[r]);
+                            T gr = MIXED ? tcv[r] + acc[i][q] : acc[i][q] - tcv[r];
                             p[i][q] = p[i][q] - gr * hstep * dts[q];
                         }
                     }
@@ -676,12 +703,11 @@ __global__ void __launch_bounds__(NT, 1) inner_kernel(MeshDev m, InnerArgs a) {
                         for (int i = 0; i < RT; ++i) {
                             int r = ty * RT + i;
                             if (live && r < D) {
-                                T cr = (T)vcov[r];
-                                x[i][q] = x[i][q] + cr * p[i][q] * xstep * dts[q];
-                                if (fabs((double)x[i][q]) > 1e3) atomicOr(&s.blown[c], 1);
+                                x[i][q] = x[i][q] + tcov[r] * p[i][q] * xstep * dts[q];
+                                if (fabs(x[i][q]) > T(1e3)) atomicOr(&s.blown[c], 1);
                                 else reflect<T>(x[i][q], p[i][q], mx, flag);
                             }
-                            T xv = MIXED ? (T)((double)x[i][q] - vmean[r < DP ? r : 0]) : x[i][q];
+                            T xv = MIXED ? x[i][q] - tmean[r] : x[i][q];
                             Xw[(size_t)r * C + c] = (r < D) ? xv : T(0);
                         }
                     }
@@ -906,6 +932,7 @@ static size_t inner_smem_bytes() {
     using TL = Tile<T, RT, CT>;
     constexpr int DP = TL::DP, C = TL::C;
     size_t b = (size_t)2 * DP * DP * sizeof(T) + (size_t)2 * DP * C * sizeof(T);
+    b += (size_t)4 * DP * sizeof(T);
     b += (size_t)6 * DP * sizeof(double) + (size_t)TYN * C * sizeof(double) + 64 * sizeof(double);
     b += (size_t)9 * C * sizeof(double) + (size_t)(6 * C + 2) * sizeof(int) + 8 * sizeof(long long) + 64;
     return b;

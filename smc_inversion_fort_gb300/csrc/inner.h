@@ -17,6 +17,7 @@ struct InnerArgs {
     const unsigned long long *streams;  // [n_theta]
     // per-theta operator data
     const double *A;      // [th][D][D] column-major Gram matrix
+    float *A32;           // [th][D][D] FP32 copy (MIXED), written by the inner kernel
     const double *b;      // [th][D]
     const double *dsd;    // [th]
     const double *lval;   // [th][nrow][9] values of L (columns in MeshDev::l_col)
@@ -36,5 +37,6 @@ struct InnerArgs {
 
 cudaError_t launch_gibbs(const MeshDev &m, const InnerArgs &a, cudaStream_t s);
 cudaError_t launch_inner(const MeshDev &m, const InnerArgs &a, cudaStream_t s, const char **why);
+cudaError_t launch_inner_warp(const MeshDev &m, const InnerArgs &a, cudaStream_t s, const char **why);
 
 }  // namespace smc

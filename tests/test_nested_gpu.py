@@ -130,6 +130,9 @@ def test_nested_mixed_matches_fp64(smcgpu, orc):
     a, b = a.reshape(-1, reps), b.reshape(-1, reps)
     se = np.sqrt((a.var(1, ddof=1) + b.var(1, ddof=1)) / reps)
     print("fp64 ", a.mean(1), "\nmixed", b.mean(1), "\nse   ", se)
+    print("fp64 std", a.std(1), "min", a.min(1), "max", a.max(1))
+    print("mixed std", b.std(1), "min", b.min(1), "max", b.max(1))
+    print("mixed worst reps", np.sort(b[-1])[-6:], "fp64", np.sort(a[-1])[-6:])
     assert np.all(np.abs(a.mean(1) - b.mean(1)) < 4 * se + 1e-9)
     assert np.all(np.abs(a.mean(1) - b.mean(1)) < 1.0)
 
