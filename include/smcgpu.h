@@ -84,6 +84,9 @@ typedef struct smcgpu_config {
     int32_t max_outer_stages;      /* stop fault_smc_exec after this many stages (0: run
                                       until gamma = 1 as the reference does; < 0: only
                                       the initial evaluation of the prior sample)       */
+    int32_t inner_warps;           /* warps per geometry particle in the inner SMC kernel:
+                                      1, 2, 4 or 8; 0 picks from the batch size. Results
+                                      do not depend on it.                              */
 } smcgpu_config;
 
 typedef struct smcgpu_ctx smcgpu_ctx;

@@ -38,6 +38,7 @@ class SmcConfig(C.Structure):
         ("max_stages", C.c_int32),
         ("cv_inner", C.c_double), ("cv_outer", C.c_double), ("sar_corr_len", C.c_double),
         ("precision", C.c_int32), ("device", C.c_int32), ("max_outer_stages", C.c_int32),
+        ("inner_warps", C.c_int32),
     ]
 
 
@@ -111,6 +112,7 @@ def make_config(s: SmcSettings, precision: int = PREC_FP64, device: int = 0) -> 
     cfg.cv_inner, cfg.cv_outer, cfg.sar_corr_len = s.cv_inner, s.cv_outer, s.sar_corr_len
     cfg.precision, cfg.device = precision, device
     cfg.max_outer_stages = s.max_outer_stages
+    cfg.inner_warps = s.inner_warps
     return cfg
 
 

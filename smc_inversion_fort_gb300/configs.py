@@ -38,6 +38,7 @@ class SmcSettings:
     cv_outer: float = 0.2
     sar_corr_len: float = 10.0
     max_outer_stages: int = 0
+    inner_warps: int = 0          # GPU inner kernel: warps per geometry (0: by batch size)
 
     def ndim_fault(self) -> int:
         if self.layout == 0:

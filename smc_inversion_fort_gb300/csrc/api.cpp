@@ -83,6 +83,9 @@ extern "C" int32_t smcgpu_create(const smcgpu_config *cfg, smcgpu_ctx **out) {
     if (e.empty() && (cfg->nparticle_slip < 2 || cfg->ntau < 1 || cfg->tuning_factor < 1 || cfg->max_stages < 0))
         e = "invalid SMC settings";
     if (e.empty() && !(cfg->max_slip > 0.0)) e = "max_slip must be positive";
+    if (e.empty() && cfg->inner_warps != 0 && cfg->inner_warps != 1 && cfg->inner_warps != 2 &&
+        cfg->inner_warps != 4 && cfg->inner_warps != 8)
+        e = "inner_warps must be 0, 1, 2, 4 or 8";
     if (!e.empty()) { g_create_err = e; delete ctx; return SMCGPU_ERR_ARG; }
     cudaError_t ce = cudaSetDevice(cfg->device);
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);

@@ -97,8 +97,8 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
         CU(smc::launch_gibbs(ctx->md, a, s), "gibbs kernel");
         const char *why = nullptr;
         a.A32 = ctx->d_A32.p;
-        static const bool use_cta = getenv("SMCGPU_INNER_CTA") != nullptr;
-        cudaError_t e = use_cta ? smc::launch_inner(ctx->md, a, s, &why) : smc::launch_inner_warp(ctx->md, a, s, &why);
+        a.warps_per_theta = ctx->cfg.inner_warps;
+        cudaError_t e = smc::launch_inner(ctx->md, a, s, &why);
         if (e != cudaSuccess) {
             if (why) return ctx->fail(SMCGPU_ERR_ARG, why);
             return ctx->cuda_fail(e, "inner kernel");

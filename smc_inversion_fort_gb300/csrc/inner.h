@@ -12,6 +12,7 @@ namespace smc {
 struct InnerArgs {
     int n_theta, N, NP2, D, mixed;
     int ntau, tf, max_stages;
+    int warps_per_theta;  // warps per geometry in the inner kernel (1, 2, 4, 8; 0 picks by batch size)
     double cv, max_slip;
     uint64_t seed;
     const unsigned long long *streams;  // [n_theta]
@@ -37,6 +38,5 @@ struct InnerArgs {
 
 cudaError_t launch_gibbs(const MeshDev &m, const InnerArgs &a, cudaStream_t s);
 cudaError_t launch_inner(const MeshDev &m, const InnerArgs &a, cudaStream_t s, const char **why);
-cudaError_t launch_inner_warp(const MeshDev &m, const InnerArgs &a, cudaStream_t s, const char **why);
 
 }  // namespace smc

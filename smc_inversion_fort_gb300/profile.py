@@ -1,7 +1,7 @@
 """Fixed small workloads for profiling one kernel family at a time.
 
     python -m smc_inversion_fort_gb300.profile greens [--n-theta 256] [--fp32] [--reps 2]
-    python -m smc_inversion_fort_gb300.profile nested [--n-theta 16] [--mixed] [--reps 1]
+    python -m smc_inversion_fort_gb300.profile nested [--n-theta 16] [--mixed] [--reps 1] [--warps 0]
 
 `greens` runs the Green's build of the 16x8-patch, 5x5-Gauss-point,
 400-station workload on n geometries; `nested` runs nested evaluations of the
@@ -22,6 +22,7 @@ def main(argv=None):
     p.add_argument("--fp32", action="store_true")
     p.add_argument("--mixed", action="store_true")
     p.add_argument("--reps", type=int, default=2)
+    p.add_argument("--warps", type=int, default=0, help="inner kernel warps per geometry (0: by batch size)")
     a = p.parse_args(argv)
     import torch
 
@@ -47,6 +48,7 @@ def main(argv=None):
             print(f"greens n_theta={n} {'fp32' if a.fp32 else 'fp64'}: {1e3 * (time.perf_counter() - t0):.2f} ms")
     else:
         w = preset("c0")
+        w.settings.inner_warps = a.warps
         n = a.n_theta or 16
         rng = np.random.default_rng(2024)
         obs = make_stations(w, rng)
@@ -61,7 +63,7 @@ def main(argv=None):
         for r in range(a.reps):
             t0 = time.perf_counter()
             nl, st = g.fault_calc_likelihood(th, 1, np.arange(n, dtype=np.uint64) + 1000 * r)
-            print(f"nested n_theta={n} {'mixed' if a.mixed else 'fp64'}: {time.perf_counter() - t0:.3f} s, "
+            print(f"nested n_theta={n} warps={a.warps} {'mixed' if a.mixed else 'fp64'}: {time.perf_counter() - t0:.3f} s, "
                   f"-logZ[0] {nl[0]:.4f}, status {int(st.max())}")
 
 
