@@ -19,6 +19,7 @@
  *   smcgpu_fault_smc_exec      smc_fault.f90:785-1075 fault_smc_exec
  *   smcgpu_resample_counts     smc_slip.f90:572-589 / smc_fault.f90:572-590
  *   smcgpu_qsort_              sort.cpp:3-7 qsort_ (same symbol shape)
+ *   smcgpu_read_*              main.f90:107-157, init.f90:5-80 (input files)
  */
 #ifndef SMCGPU_H
 #define SMCGPU_H
@@ -45,6 +46,8 @@ extern "C" {
 #define SMCGPU_ST_NEWTON_CAP   8   /* inverse-CDF Newton loop hit 100 iterations       */
 #define SMCGPU_ST_REFLECT_CAP 16   /* reflection loop hit its cap                      */
 #define SMCGPU_ST_TUNE_COUNT  32   /* step-size resampling count != N                  */
+#define SMCGPU_ST_WAIT_CAP    64   /* a bounded device wait (tensor-core completion)
+                                      gave up; the evaluation was abandoned, neglog = 1e10 */
 
 /* theta layouts */
 #define SMCGPU_LAYOUT_TRACE          0  /* [ymin ymax (x_i y_i)_{i<nplane} dip_1..n la2 ls_sar ls_gnss] (init.f90:152-167) */
@@ -59,6 +62,11 @@ extern "C" {
 #define SMCGPU_PREC_FP64   0   /* FP64 everywhere, reference operation order          */
 #define SMCGPU_PREC_FP32   1   /* Green's build only: FP32 arithmetic, float output    */
 #define SMCGPU_PREC_MIXED  2   /* nested SMC: FP32 leapfrog, FP64 likelihood/evidence  */
+
+/* inner SMC step engines (smcgpu_config.inner_engine, MIXED only) */
+#define SMCGPU_ENGINE_MMA      0   /* BF16x3 mma.sync tiles, FP32 accumulate (default)  */
+#define SMCGPU_ENGINE_CUDA     1   /* FP32 FMA on CUDA cores                            */
+#define SMCGPU_ENGINE_TCGEN05  2   /* BF16x3 tcgen05.mma with a tensor-memory accumulator */
 
 typedef struct smcgpu_config {
     int32_t layout;
@@ -84,9 +92,13 @@ typedef struct smcgpu_config {
     int32_t max_outer_stages;      /* stop fault_smc_exec after this many stages (0: run
                                       until gamma = 1 as the reference does; < 0: only
                                       the initial evaluation of the prior sample)       */
-    int32_t inner_warps;           /* warps per geometry particle in the inner SMC kernel:
-                                      1, 2, 4 or 8; 0 picks from the batch size. Results
-                                      do not depend on it.                              */
+    int32_t inner_warps;           /* CUDA-core inner SMC engine: warps per geometry
+                                      particle, 1, 2, 4 or 8; 0 picks from the batch size.
+                                      Results do not depend on it.                      */
+    int32_t inner_engine;          /* MIXED leapfrog engine, SMCGPU_ENGINE_*: warp-level
+                                      tensor-core MMA (default), CUDA cores, or tcgen05;
+                                      the tensor-core engines take slip dimensions <= 128
+                                      and fall back to CUDA cores above                 */
 } smcgpu_config;
 
 typedef struct smcgpu_ctx smcgpu_ctx;
@@ -186,7 +198,58 @@ int32_t smcgpu_resample_counts(smcgpu_ctx *ctx, const double *weights, int32_t n
  * by arr[index-1] descending with the same std::sort comparator. */
 void smcgpu_qsort_(int32_t *arr, int32_t *index, int32_t *n);
 
-/* Last error message of the context (or of the last create call when ctx is NULL). */
+/* ---- readers for the reference's input files (host only; no GPU needed).
+ * Fortran list-directed semantics: blank/comma separated values that may
+ * continue over records, r*v repeats, D exponents, .true./T/.false./F. */
+#define SMCGPU_PATH_MAX 512
+typedef struct smcgpu_settings {
+    int32_t nplane;
+    int32_t fix_xbend;                   /* logical */
+    double xbend[SMCGPU_MAX_PLANES];     /* nplane-1 values */
+    int32_t nparticle_fault;
+    int32_t nparticle_slip;
+    char observation_path[SMCGPU_PATH_MAX];
+    int32_t npath;                       /* number of InSAR paths */
+    char output_dir[SMCGPU_PATH_MAX];
+    double max_slip;
+    int32_t nxi[SMCGPU_MAX_PLANES];
+    int32_t neta[SMCGPU_MAX_PLANES];
+    double xmin, xmax, zmin;
+    int32_t gsmc;                        /* logical */
+} smcgpu_settings;
+
+/* data/setting.dat (main.f90:107-157). */
+int32_t smcgpu_read_settings(const char *path, smcgpu_settings *out);
+/* The context configuration the reference derives from the settings:
+ * nodal basis, trace layout with or without fixed bends, reference constants. */
+int32_t smcgpu_settings_to_config(const smcgpu_settings *st, smcgpu_config *cfg);
+/* read_observation1 (init.f90:5-22): number of observation rows (records
+ * after the header). */
+int32_t smcgpu_count_observations(const char *path, int32_t *nobs);
+/* read_observation2 (init.f90:24-80): rows "x y ex ey ez dlos sigma type";
+ * consecutive "InSAR*" rows of one type form a path, "GNSS" rows come in
+ * station triples.  obs_points 2 x nobs, obs_unitvec 3 x nobs (column-major),
+ * nsar_index npath+1 (1-based, as the reference). */
+int32_t smcgpu_read_observations(const char *path, int32_t nobs, int32_t npath, double *obs_points,
+                                 double *obs_unitvec, double *obs_sigma, double *dvec, int32_t *nsar_index,
+                                 int32_t *nsar_total, int32_t *ngnss);
+/* data/range.dat (main.f90:497-502): per parameter a label record then
+ * "lower upper"; range is 2 x ndim (column-major). */
+int32_t smcgpu_read_range(const char *path, int32_t ndim, double *range);
+/* A plain list of n reals: one READ per value (peak_fault.dat, main.f90:430-434)
+ * when one_per_record, else one list-directed READ of all n (qmean.dat,
+ * qcov.dat, main.f90:313-330). */
+int32_t smcgpu_read_values(const char *path, int32_t n, int32_t one_per_record, double *out);
+
+/* slip_smc_exec's posterior dump (smc_slip.f90:1632-1660): one record per
+ * particle with the two slip components of every node (0 where the node has
+ * no DOF), then likelihood and prior, Fortran f12.5.  particles is D x
+ * nparticle (column-major), e.g. from smcgpu_fault_likelihood_posterior. */
+int32_t smcgpu_write_slip(smcgpu_ctx *ctx, const char *path, int32_t nparticle, const double *particles,
+                          const double *likelihood, const double *prior);
+
+/* Last error message of the context (or, when ctx is NULL, of the last
+ * create call or file reader on this thread). */
 const char *smcgpu_last_error(const smcgpu_ctx *ctx);
 
 #ifdef __cplusplus

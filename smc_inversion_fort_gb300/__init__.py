@@ -23,6 +23,8 @@ LAYOUT_TRACE, LAYOUT_TRACE_FIXBEND, LAYOUT_RECT = 0, 1, 2
 BASIS_NODAL, BASIS_PATCH = 0, 1
 PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
 ST_BISECT_CAP, ST_STAGE_CAP, ST_NONFINITE, ST_NEWTON_CAP, ST_REFLECT_CAP, ST_TUNE_COUNT = 1, 2, 4, 8, 16, 32
+ST_WAIT_CAP = 64
+ENGINE_MMA, ENGINE_CUDA, ENGINE_TCGEN05 = 0, 1, 2
 
 
 class SmcConfig(C.Structure):
@@ -38,7 +40,21 @@ class SmcConfig(C.Structure):
         ("max_stages", C.c_int32),
         ("cv_inner", C.c_double), ("cv_outer", C.c_double), ("sar_corr_len", C.c_double),
         ("precision", C.c_int32), ("device", C.c_int32), ("max_outer_stages", C.c_int32),
-        ("inner_warps", C.c_int32),
+        ("inner_warps", C.c_int32), ("inner_engine", C.c_int32),
+    ]
+
+
+PATH_MAX = 512
+
+
+class SettingsFile(C.Structure):
+    """smcgpu_settings: the values of the reference's data/setting.dat."""
+    _fields_ = [
+        ("nplane", C.c_int32), ("fix_xbend", C.c_int32), ("xbend", C.c_double * MAX_PLANES),
+        ("nparticle_fault", C.c_int32), ("nparticle_slip", C.c_int32),
+        ("observation_path", C.c_char * PATH_MAX), ("npath", C.c_int32), ("output_dir", C.c_char * PATH_MAX),
+        ("max_slip", C.c_double), ("nxi", C.c_int32 * MAX_PLANES), ("neta", C.c_int32 * MAX_PLANES),
+        ("xmin", C.c_double), ("xmax", C.c_double), ("zmin", C.c_double), ("gsmc", C.c_int32),
     ]
 
 
@@ -72,6 +88,13 @@ def load_library() -> C.CDLL:
         "smcgpu_resample_counts": (i32, [vp, vp, i32, d, d, vp]),
         "smcgpu_qsort_": (None, [vp, vp, vp]),
         "smcgpu_last_error": (C.c_char_p, [vp]),
+        "smcgpu_read_settings": (i32, [C.c_char_p, P(SettingsFile)]),
+        "smcgpu_settings_to_config": (i32, [P(SettingsFile), P(SmcConfig)]),
+        "smcgpu_count_observations": (i32, [C.c_char_p, P(i32)]),
+        "smcgpu_read_observations": (i32, [C.c_char_p, i32, i32, vp, vp, vp, vp, vp, P(i32), P(i32)]),
+        "smcgpu_read_range": (i32, [C.c_char_p, i32, vp]),
+        "smcgpu_read_values": (i32, [C.c_char_p, i32, i32, vp]),
+        "smcgpu_write_slip": (i32, [vp, C.c_char_p, i32, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -86,7 +109,8 @@ EXPORTED_SYMBOLS = [
     "smcgpu_dims", "smcgpu_greens_batch", "smcgpu_greens_batch_dev", "smcgpu_fault_likelihood_batch",
     "smcgpu_fault_likelihood_batch_dev", "smcgpu_fault_likelihood_trace", "smcgpu_fault_likelihood_posterior",
     "smcgpu_fault_smc_exec", "smcgpu_resample_counts", "smcgpu_qsort_",
-    "smcgpu_last_error",
+    "smcgpu_last_error", "smcgpu_read_settings", "smcgpu_settings_to_config", "smcgpu_count_observations",
+    "smcgpu_read_observations", "smcgpu_read_range", "smcgpu_read_values", "smcgpu_write_slip",
 ]
 
 
@@ -113,6 +137,7 @@ def make_config(s: SmcSettings, precision: int = PREC_FP64, device: int = 0) -> 
     cfg.precision, cfg.device = precision, device
     cfg.max_outer_stages = s.max_outer_stages
     cfg.inner_warps = s.inner_warps
+    cfg.inner_engine = s.inner_engine
     return cfg
 
 
@@ -221,6 +246,13 @@ class SmcGpu:
     def fault_likelihood_dev(self, n, theta_ptr, seed, streams_ptr, neglog_ptr, status_ptr):
         self._check(self.lib.smcgpu_fault_likelihood_batch_dev(self.h, n, theta_ptr, seed, streams_ptr, neglog_ptr,
                                                                status_ptr), "fault_likelihood_batch_dev")
+
+    def write_slip(self, path: str, particles: np.ndarray, likelihood: np.ndarray, prior: np.ndarray):
+        """slip_smc_exec's posterior dump (smc_slip.f90:1632-1660)."""
+        x = np.ascontiguousarray(particles, dtype=np.float64)
+        L = np.ascontiguousarray(likelihood, dtype=np.float64)
+        P = np.ascontiguousarray(prior, dtype=np.float64)
+        self._check(self.lib.smcgpu_write_slip(self.h, path.encode(), len(L), _ptr(x), _ptr(L), _ptr(P)), "write_slip")
 
     # fault_smc_exec (smc_fault.f90:785-1075)
     def fault_smc_exec(self, range_: np.ndarray, nparticle: int, seed: int, output_dir: str | None = None):

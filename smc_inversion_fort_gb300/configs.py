@@ -39,6 +39,7 @@ class SmcSettings:
     sar_corr_len: float = 10.0
     max_outer_stages: int = 0
     inner_warps: int = 0          # GPU inner kernel: warps per geometry (0: by batch size)
+    inner_engine: int = 0         # MIXED inner step engine: 0 warp MMA, 1 CUDA cores, 2 tcgen05
 
     def ndim_fault(self) -> int:
         if self.layout == 0:

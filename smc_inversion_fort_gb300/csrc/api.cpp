@@ -10,7 +10,10 @@
 
 using smc::DevBuf;
 
-static thread_local std::string g_create_err;
+namespace smc {
+thread_local std::string g_create_err;
+}
+using smc::g_create_err;
 
 #define CU(call, where)                                  \
     do {                                                 \
@@ -86,6 +89,8 @@ extern "C" int32_t smcgpu_create(const smcgpu_config *cfg, smcgpu_ctx **out) {
     if (e.empty() && cfg->inner_warps != 0 && cfg->inner_warps != 1 && cfg->inner_warps != 2 &&
         cfg->inner_warps != 4 && cfg->inner_warps != 8)
         e = "inner_warps must be 0, 1, 2, 4 or 8";
+    if (e.empty() && (cfg->inner_engine < SMCGPU_ENGINE_MMA || cfg->inner_engine > SMCGPU_ENGINE_TCGEN05))
+        e = "inner_engine must be SMCGPU_ENGINE_MMA, _CUDA or _TCGEN05";
     if (!e.empty()) { g_create_err = e; delete ctx; return SMCGPU_ERR_ARG; }
     cudaError_t ce = cudaSetDevice(cfg->device);
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);

@@ -10,6 +10,16 @@
 #include "kernels.h"
 #include "mesh.h"
 
+namespace smc {
+// message of the last call that had no context (create, the file readers)
+extern thread_local std::string g_create_err;
+// Fortran "Fw.d" edit descriptor: right-aligned in w columns, w asterisks
+// when the value does not fit, NaN / Infinity spelled as gfortran does
+std::string fortran_f(double v, int w, int d);
+// "mkdir -p" of a path (the reference shells out to it, main.f90:202-207)
+void mkdir_p(const std::string &path);
+}
+
 struct smcgpu_ctx {
     smcgpu_config cfg;
     smc::MeshPattern mesh;

@@ -98,6 +98,7 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
         const char *why = nullptr;
         a.A32 = ctx->d_A32.p;
         a.warps_per_theta = ctx->cfg.inner_warps;
+        a.engine = ctx->cfg.inner_engine;
         cudaError_t e = smc::launch_inner(ctx->md, a, s, &why);
         if (e != cudaSuccess) {
             if (why) return ctx->fail(SMCGPU_ERR_ARG, why);
@@ -253,13 +254,18 @@ static double host_normal(uint64_t seed, uint64_t stream, uint32_t purpose, uint
 
 static void write_stage_csv(const char *dir, int iter, const std::vector<double> &parts, const std::vector<double> &L,
                             int N, int nd) {
-    // smc_fault.f90:923-936 / 1054-1067: ndim columns + likelihood, f20.5
-    std::string path = std::string(dir) + "/" + std::to_string(iter) + ".csv";
+    // smc_fault.f90:923-936 / 1054-1067: file trim(output_dir)//iter//".csv",
+    // one record per particle: ndim values and the likelihood, each f20.5
+    std::string path = std::string(dir) + std::to_string(iter) + ".csv";
     FILE *f = std::fopen(path.c_str(), "w");
     if (!f) return;
+    std::string line;
     for (int i = 0; i < N; ++i) {
-        for (int d = 0; d < nd; ++d) std::fprintf(f, "%20.5f", parts[(size_t)i * nd + d]);
-        std::fprintf(f, "%20.5f\n", L[i]);
+        line.clear();
+        for (int d = 0; d < nd; ++d) line += smc::fortran_f(parts[(size_t)i * nd + d], 20, 5);
+        line += smc::fortran_f(L[i], 20, 5);
+        line += '\n';
+        std::fputs(line.c_str(), f);
     }
     std::fclose(f);
 }
@@ -272,7 +278,7 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
     if (r) return r;
     if (!range || N < 2 || !evidence_out) return ctx->fail(SMCGPU_ERR_ARG, "fault_smc_exec: bad arguments");
     CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
-    if (output_dir) mkdir(output_dir, 0755);
+    if (output_dir) smc::mkdir_p(output_dir);
     const int nd = ctx->mesh.ndim_fault;
     const uint64_t OS = smc::OUTER_STREAM;
     cudaStream_t s = ctx->stream;

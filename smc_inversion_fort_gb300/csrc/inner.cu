@@ -1,42 +1,80 @@
 // Inner tempered SMC over slip (slip_smc_exec, smc_slip.f90:1445-1663):
-// one GROUP of W warps per geometry particle, G = 8/W groups per CTA.
+// one GROUP of W warps per geometry particle, persistent over all stages.
 //
 // The HMC children of one parent form a Metropolis chain
 // (smc_slip.f90:591-730: child k starts where child k-1 stopped), so an
-// inner stage is a set of chains of uneven length.  Every warp of a group
-// runs C = 8 chain slots in lock step and refills a slot from the group's
-// parent queue (sorted by descending child count) when its chain ends.  A
-// leapfrog step of a warp's 8 slots is the product grad = M x of the stage
-// matrix M = gamma A + L^T L / alpha^2 (shared memory, one copy per group)
-// with the warp's DP x 8 slot tile; lane l owns rows (l%16)*RT.. and slots
-// (l/16)*4.. and applies the momentum / position update, the reflection into
-// [0, max_slip] and the blow-up test to its own entries, so a step needs no
-// synchronisation beyond the warp.  The warps of a group meet only at stage
-// boundaries (named barrier per group).  W trades per-geometry latency
-// (more slots: fewer rounds per stage) against geometries per SM; the host
-// picks it from the batch size.  Random draws are addressed by (stage,
-// purpose, child index, dimension): the slot schedule does not change results.
+// inner stage is a set of chains of uneven length.  A group runs chain slots
+// in lock step and refills a slot from the group's parent queue (sorted by
+// descending child count) when its chain ends.  A leapfrog step of all slots
+// is the product grad = M x of the stage matrix M = gamma A + L^T L / alpha^2
+// with the slot tile x, followed by the element-wise momentum / position
+// update, the reflection into [0, max_slip] and the blow-up test.  Random
+// draws are addressed by (stage, purpose, child index, dimension), so the
+// slot schedule does not change results.
+//
+// Two step engines share the stage-level code (bisection, normalisation,
+// moments, resampling counts, parent queue, step-size tuning):
+//
+//  * CUDA cores (FP64, and MIXED with D > 128): every warp of a group owns
+//    C = 8 slots and runs its own FMA GEMM M x out of shared memory (lane l
+//    owns rows (l%16)*RT.. and slots (l/16)*4..), so a step needs no
+//    synchronisation beyond the warp.  W = 1..8 warps per geometry, chosen
+//    from the batch size.
+//
+//  * Tensor cores (MIXED, D <= 128): one warpgroup per geometry.  M is split
+//    into BF16 hi + lo (stacked 128/DP times to fill the 128-row MMA) and the
+//    slot tile's offsets from the stage mean likewise; thread 0 issues
+//    hi*hi + hi*lo + lo*hi as tcgen05.mma (M = 128, N = 2048/DP slots, K = 16
+//    per instruction) into a tensor-memory accumulator, and every thread
+//    reads back its row (one dimension) for 16 slots with tcgen05.ld.  The
+//    gradient error is O(2^-16) relative; the Metropolis test is exact for
+//    any deterministic gradient, and the end-point energies keep their FP32 /
+//    FP64 form, so only the acceptance rate can move.
 //
 // FP64 (T = double) follows the reference's algebra in FP64.  MIXED
-// (T = float) runs the leapfrog in FP32 about the stage mean sbar with the
-// constant part of the gradient and the end-point energies formed in FP64,
-// and the tempering bisection in FP32 before one FP64 pass for the weights
-// and the evidence increment.
+// (T = float) runs the leapfrog in FP32 (or the tensor cores) about the stage
+// mean sbar with the constant part of the gradient and the end-point energies
+// formed in FP64, and the tempering bisection in FP32 before one FP64 pass
+// for the weights and the evidence increment.
+#include <algorithm>
 #include <type_traits>
 
 #include "common.cuh"
 #include "ddreal.cuh"
 #include "inner.h"
 #include "q128.cuh"
+#include "tc.cuh"
 
 namespace smc {
 
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int CW = 8;    // chain slots per warp
+constexpr int CW = 8;    // chain slots per warp (CUDA-core engine)
 constexpr int CTW = 4;   // slots per lane
 constexpr int RGW = 16;  // row groups per warp
+constexpr uint32_t WAIT_TRIES = 1u << 22;   // bounded mbarrier wait
+enum : int { ENG_CC = 0, ENG_TC = 1, ENG_MMA = 2 };   // step engines
+
+// ---- warp-level tensor-core MMA (BF16 in, FP32 accumulate), m16n8k16
+__device__ __forceinline__ void ldsm_x4(uint32_t r[4], const void *p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(tc::smem_u32(p)));
+}
+__device__ __forceinline__ void ldsm_x2_t(uint32_t r[2], const void *p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];"
+                 : "=r"(r[0]), "=r"(r[1])
+                 : "r"(tc::smem_u32(p)));
+}
+__device__ __forceinline__ void mma16816(float d[4], const uint32_t a[4], const uint32_t b[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+__device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t *>(&v); }
 
 __device__ __forceinline__ double wsum(double v) {
 #pragma unroll
@@ -93,6 +131,21 @@ __device__ __forceinline__ void reflect_w(T &x, T &p, T mx, int &flag) {
         if (++it > 1000000) { flag |= SMCGPU_ST_REFLECT_CAP; break; }
     }
 }
+// Sum of 16 per-slot values over the 32 lanes of a warp: afterwards lane l
+// holds the total of slot l >> 1 (in v[0]); 16 exchanges instead of 80.
+__device__ __forceinline__ double wreduce16(double v[16], int lane) {
+#pragma unroll
+    for (int o = 16, n = 16; o >= 2; o >>= 1, n >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < n / 2; ++i) {
+            double send = up ? v[i] : v[i + n / 2];
+            double keep = up ? v[i + n / 2] : v[i];
+            v[i] = keep + __shfl_xor_sync(FULL, send, o);
+        }
+    }
+    return v[0] + __shfl_xor_sync(FULL, v[0], 1);
+}
 
 // Group of W warps (W*32 threads) synchronised by named barrier id+1.
 struct Group {
@@ -114,6 +167,19 @@ struct Group {
         double t = 0.0;
         for (int w = 0; w < W; ++w) t += scr[w];
         return t;
+    }
+    // two sums in one round of barriers
+    __device__ void sum2(double &u, double &v) const {
+        u = wsum(u);
+        v = wsum(v);
+        if (W == 1) return;
+        sync();
+        if (lane == 0) { scr[wl] = u; scr[W + wl] = v; }
+        sync();
+        double tu = 0.0, tv = 0.0;
+        for (int w = 0; w < W; ++w) { tu += scr[w]; tv += scr[W + w]; }
+        u = tu;
+        v = tv;
     }
     __device__ double min(double v) const {
         v = wmin(v);
@@ -206,52 +272,98 @@ __device__ __forceinline__ void warp_gemm(const T *__restrict__ Mcol, const T *_
     }
 }
 
-// shared memory of one group
-template <typename T, int RT>
-struct GroupSmem {
+// ---- shared memory of one group
+//
+// CUDA-core engine: M (DP x DP, T), W double-buffered DP x 8 slot tiles.
+// tcgen05 engine: A hi/lo (128 x DP BF16 core-matrix operands), B hi/lo
+// (S x DP), the FP32 end-point tile Xf (DP x S) aliasing B.
+// Warp-MMA engine: A hi/lo (DP x DP, row stride DP+8), two B buffers hi/lo
+// (DP x S, row stride S+8), FP32 tiles X, P, XC (DP x S, row stride S+1);
+// the end-point offsets tile aliases the idle B buffer.
+// All: per-dimension T and double arrays, per-slot state, scratch.
+template <typename T, int RT, int ENG>
+struct Layout {
     static constexpr int DP = RGW * RT;
+    static constexpr int S = ENG == ENG_CC ? CW : 2048 / DP;   // slots per warp (CC) / per group
+    static constexpr uint32_t LBO_A = 2048;              // tcgen05: 128 rows x 16 B per k block
+    static constexpr uint32_t LBO_B = 16 * S + 16;       // tcgen05: S rows x 16 B per k block, padded
+    static constexpr size_t A_BYTES = ENG == ENG_TC ? (size_t)LBO_A * (DP / 8) : (size_t)DP * (DP + 8) * 2;
+    static constexpr size_t B_BYTES = ENG == ENG_TC ? (size_t)LBO_B * (DP / 8) : (size_t)DP * (S + 8) * 2;
+    static constexpr int AST = DP + 8, BST = S + 8, TS = S + 1;   // warp-MMA row strides (elements)
+    static constexpr size_t TILE_BYTES = (size_t)DP * TS * sizeof(float);
+    __host__ __device__ static size_t engine_bytes(int W) {
+        if (ENG == ENG_TC) return 2 * A_BYTES + 2 * B_BYTES;   // the end-point tile Xf aliases B
+        if (ENG == ENG_MMA)   // + the FP32 Gram matrix for the end-point energies
+            return 2 * A_BYTES + 4 * B_BYTES + 3 * TILE_BYTES + (size_t)DP * DP * sizeof(float);
+        return (size_t)DP * DP * sizeof(T) + (size_t)W * 2 * DP * CW * sizeof(T);
+    }
+    __host__ __device__ static int slots(int W) { return ENG == ENG_CC ? W * CW : S; }
     __host__ __device__ static size_t bytes(int W) {
-        return (size_t)DP * DP * sizeof(T) + (size_t)W * 2 * DP * CW * sizeof(T) + (size_t)4 * DP * sizeof(T) +
-               (size_t)6 * DP * sizeof(double) + (size_t)W * CW * (5 * sizeof(double) + 5 * sizeof(int)) +
-               (size_t)(4 * W + 8) * sizeof(double);
+        size_t b = engine_bytes(W) + (size_t)4 * DP * sizeof(T) + (size_t)6 * DP * sizeof(double) +
+                   (size_t)slots(W) * (5 * sizeof(double) + 5 * sizeof(int)) + (size_t)(4 * W + 8) * sizeof(double);
+        if (ENG != ENG_CC) b += (size_t)5 * 32 * (W > 4 ? W : 4) * sizeof(double) + 64;   // reductions, masks, mbarrier
+        return (b + 127) & ~(size_t)127;
     }
 };
 
 }  // namespace
 
-template <typename T, int RT>
-__global__ void __launch_bounds__(256) inner_group_kernel(MeshDev m, InnerArgs a, int W, int G) {
-    constexpr int DP = RGW * RT;
+template <typename T, int RT, int ENG, int WG>
+__device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a, Group &grp, int th,
+                                           unsigned char *smem, uint32_t tmem_base) {
+    using L_ = Layout<T, RT, ENG>;
+    constexpr int DP = L_::DP;
     constexpr bool MIXED = std::is_same<T, float>::value;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    Group grp;
-    grp.id = warp / W;
-    grp.W = W;
-    grp.wl = warp % W;
-    grp.lane = lane;
-    grp.gt = grp.wl * 32 + lane;
-    grp.nt = 32 * W;
-    const int th = blockIdx.x * G + grp.id;
-    if (grp.id >= G || th >= a.n_theta) return;
+    constexpr bool TC = ENG == ENG_TC;
+    static_assert(ENG == ENG_CC || MIXED, "tensor-core engines are MIXED only");
+    const int lane = grp.lane;
     const int N = a.N, D = a.D, NP2 = a.NP2;
-    const int rg = lane & 15, cg = lane >> 4, gt = grp.gt, gnt = grp.nt, wl = grp.wl;
+    const int rg = lane & 15, cg = lane >> 4, gt = grp.gt, gnt = grp.nt, wl = grp.wl, W = grp.W;
+    const int NS = L_::slots(W);
 
-    extern __shared__ __align__(16) unsigned char smem_all[];
-    unsigned char *smem = smem_all + (size_t)grp.id * GroupSmem<T, RT>::bytes(W);
-    T *Msm = (T *)smem;
-    T *Xw0 = Msm + DP * DP + (size_t)wl * 2 * DP * CW, *Xw1 = Xw0 + DP * CW;   // this warp's tiles
-    T *tcov = Msm + DP * DP + (size_t)W * 2 * DP * CW, *tmean = tcov + DP, *tcv = tmean + DP, *tisc = tcv + DP;
+    // ---- shared memory carve-up
+    unsigned char *sp = smem;
+    T *Msm = nullptr, *Xw0 = nullptr, *Xw1 = nullptr;
+    unsigned char *Ahi = nullptr, *Alo = nullptr, *Bhi = nullptr, *Blo = nullptr;
+    float *Xf = nullptr, *tX = nullptr, *tP = nullptr, *tXC = nullptr, *tA32 = nullptr;
+    if constexpr (ENG == ENG_MMA) {
+        // B buffer b: hi at Bhi + 2*b*B_BYTES, lo B_BYTES after it
+        Ahi = sp; Alo = Ahi + L_::A_BYTES; Bhi = Alo + L_::A_BYTES; Blo = Bhi + L_::B_BYTES;
+        tX = (float *)(Bhi + 4 * L_::B_BYTES);
+        tP = (float *)((unsigned char *)tX + L_::TILE_BYTES);
+        tXC = (float *)((unsigned char *)tP + L_::TILE_BYTES);
+        tA32 = (float *)((unsigned char *)tXC + L_::TILE_BYTES);
+        static_assert(2 * L_::B_BYTES >= L_::TILE_BYTES, "offset tile must fit in one B buffer");
+    } else if constexpr (TC) {
+        Ahi = sp; Alo = Ahi + L_::A_BYTES; Bhi = Alo + L_::A_BYTES; Blo = Bhi + L_::B_BYTES;
+        Xf = (float *)Bhi;   // written at the last leapfrog step, after the last MMA read B
+        static_assert(2 * L_::B_BYTES >= (size_t)DP * L_::S * sizeof(float), "Xf must fit in B");
+    } else {
+        Msm = (T *)sp;
+        Xw0 = Msm + DP * DP + (size_t)wl * 2 * DP * CW;
+        Xw1 = Xw0 + DP * CW;
+    }
+    sp += L_::engine_bytes(W);
+    T *tcov = (T *)sp, *tmean = tcov + DP, *tcv = tmean + DP, *tisc = tcv + DP;
     double *vb = (double *)(tisc + DP);
     double *vcov = vb + DP, *vmean = vcov + DP, *vg = vmean + DP, *vh = vg + DP, *vc = vh + DP;
-    double *sdall = vc + DP;                                   // W * 5 * CW doubles
-    double *sd = sdall + (size_t)wl * 5 * CW;
-    double *sL = sd, *sP = sd + CW, *spost = sd + 2 * CW, *sham = sd + 3 * CW, *sdt = sd + 4 * CW;
-    int *siall = (int *)(sdall + (size_t)W * 5 * CW);        // W * 5 * CW ints
-    int *si = siall + (size_t)wl * 5 * CW;
-    int *spar = si, *sj = si + CW, *sjend = si + 2 * CW, *sfresh = si + 3 * CW, *sblown = si + 4 * CW;
-    double *gscr = (double *)(siall + (size_t)W * 5 * CW + ((W * 5 * CW) & 1));
-    int *gint = (int *)(gscr + 4 * W);                          // [0] queue head, [1] queue length, [2] status
+    double *sdall = vc + DP;                                   // NS * 5 doubles
+    int *siall = (int *)(sdall + (size_t)NS * 5);              // NS * 5 ints
+    double *gscr = (double *)(siall + (size_t)NS * 5 + ((NS * 5) & 1));
+    int *gint = (int *)(gscr + 4 * W);   // [0] queue head, [2] status, [3] wait gave up
     grp.scr = gscr;
+    // per-warp (CC) or per-group (TC) slot state
+    const int sbase = ENG != ENG_CC ? 0 : wl * CW;
+    double *sL = sdall + sbase, *sP = sL + NS, *spost = sP + NS, *sham = spost + NS, *sdt = sham + NS;
+    int *spar = siall + sbase, *sj = spar + NS, *sjend = sj + NS, *sfresh = sjend + NS, *sblown = sfresh + NS;
+    double *red = nullptr;
+    unsigned long long *masks = nullptr;   // [0] fresh, [1] active, [2] blown, [3] accepted
+    uint64_t *mbar = nullptr;
+    if constexpr (ENG != ENG_CC) {
+        red = (double *)(gint + 8);   // [5][32 W] per-slot partial sums
+        masks = (unsigned long long *)(red + 5 * 32 * (W > 4 ? W : 4));
+        mbar = (uint64_t *)(masks + 4);
+    }
 
     const double *Ath = a.A + (size_t)th * D * D;
     const double *bth = a.b + (size_t)th * D;
@@ -268,12 +380,22 @@ __global__ void __launch_bounds__(256) inner_group_kernel(MeshDev m, InnerArgs a
     float *A32 = a.A32 ? a.A32 + (size_t)th * D * D : nullptr;
     const T mx = (T)a.max_slip;
     int status = 0;
+    uint32_t phase = 0;   // TC: parity of the next mbarrier phase
 
-    if (gt == 0) gint[2] = 0;
+    if (gt == 0) { gint[2] = 0; gint[3] = 0; }
+    if constexpr (TC) {
+        if (gt == 0) tc::mbar_init(mbar, 1);
+    }
     for (int i = gt; i < DP; i += gnt) vb[i] = i < D ? bth[i] : 0.0;
     for (int k = gt; k < N; k += gnt) dtau[k] = exp(-5.0);
-    if (MIXED)
+    if constexpr (ENG == ENG_MMA) {
+        for (int e = gt; e < DP * DP; e += gnt) {
+            const int k = e / DP, r = e % DP;
+            tA32[e] = (k < D && r < D) ? (float)Ath[(size_t)k * D + r] : 0.0f;
+        }
+    } else if (MIXED) {
         for (int e = gt; e < D * D; e += gnt) A32[e] = (float)Ath[e];
+    }
     grp.sync();
 
     // initial likelihoods and priors, FP64 Gram form (smc_slip.f90:273-286)
@@ -315,18 +437,36 @@ __global__ void __launch_bounds__(256) inner_group_kernel(MeshDev m, InnerArgs a
         double lower = gprev, upper = 1.0, err = 1.0, g = 1.0;
         int bcnt = 0;
         const double tol = MIXED ? 1e-6 : 1e-10;
+        // MIXED: this thread's first LR likelihood offsets held in registers
+        constexpr int LR = 4;
+        float lr[LR];
+        if (MIXED) {
+#pragma unroll
+            for (int q = 0; q < LR; ++q) {
+                const int k = gt + q * gnt;
+                lr[q] = k < N ? (float)(Lc[k] - lmin) : 0.0f;
+            }
+        }
         while (err > tol) {
             g = (lower + upper) / 2.0;
             double dg = g - gprev, cv;
             if (MIXED) {
                 float dgf = (float)dg;
                 double ps = 0.0, ps2 = 0.0;
-                for (int k = gt; k < N; k += gnt) {
+#pragma unroll
+                for (int q = 0; q < LR; ++q)
+                    if (gt + q * gnt < N) {
+                        float wk = expf(-dgf * lr[q]);
+                        ps += wk;
+                        ps2 += (double)wk * wk;
+                    }
+                for (int k = gt + LR * gnt; k < N; k += gnt) {
                     float wk = expf(-dgf * (float)(Lc[k] - lmin));
                     ps += wk;
                     ps2 += (double)wk * wk;
                 }
-                double s1 = grp.sum(ps), s2 = grp.sum(ps2);
+                grp.sum2(ps, ps2);
+                double s1 = ps, s2 = ps2;
                 double mean = s1 / N;
                 cv = sqrt(fmax(s2 / N - mean * mean, 0.0)) / mean;
             } else {
@@ -418,17 +558,55 @@ __global__ void __launch_bounds__(256) inner_group_kernel(MeshDev m, InnerArgs a
                 carry += tot;
             }
         }
-        // ---- stage matrix and centring terms
-        for (int e = gt; e < DP * DP; e += gnt) {
-            int i = e % DP, k = e / DP;
-            Msm[e] = (i < D && k < D) ? (T)(gamma * Ath[(size_t)k * D + i]) : T(0);
-        }
-        grp.sync();
-        for (int i = gt; i < D; i += gnt)
-            for (int e = m.ll_ptr[i]; e < m.ll_ptr[i + 1]; ++e) {
-                int k = m.ll_col[e];
-                Msm[k * DP + i] = (T)((double)Msm[k * DP + i] + llv[e] / alpha2);
+        // ---- stage matrix
+        if constexpr (ENG == ENG_MMA) {
+            // M row i split into BF16 hi + lo, row-major with row stride DP+8
+            for (int i = gt; i < DP; i += gnt) {
+                int e = i < D ? m.ll_ptr[i] : 0;
+                const int e1 = i < D ? m.ll_ptr[i + 1] : 0;
+                __nv_bfloat16 *rh = (__nv_bfloat16 *)Ahi + (size_t)i * L_::AST;
+                __nv_bfloat16 *rl = (__nv_bfloat16 *)Alo + (size_t)i * L_::AST;
+                for (int k = 0; k < DP; ++k) {
+                    double v = 0.0;
+                    if (i < D && k < D) {
+                        v = gamma * Ath[(size_t)k * D + i];
+                        while (e < e1 && m.ll_col[e] < k) ++e;
+                        if (e < e1 && m.ll_col[e] == k) v += llv[e] / alpha2;
+                    }
+                    tc::split_bf16((float)v, rh[k], rl[k]);
+                }
             }
+        } else if constexpr (TC) {
+            // row t of the 128-row A operand is M's row t % DP, split into BF16 hi + lo
+            const int i = gt % DP;
+            int e = i < D ? m.ll_ptr[i] : 0;
+            const int e1 = i < D ? m.ll_ptr[i + 1] : 0;
+            for (int k = 0; k < DP; ++k) {
+                double v = 0.0;
+                if (i < D && k < D) {
+                    v = gamma * Ath[(size_t)k * D + i];
+                    while (e < e1 && m.ll_col[e] < k) ++e;
+                    if (e < e1 && m.ll_col[e] == k) v += llv[e] / alpha2;
+                }
+                __nv_bfloat16 hi, lo;
+                tc::split_bf16((float)v, hi, lo);
+                const uint32_t off = tc::core_offset(gt, k, L_::LBO_A);
+                *(__nv_bfloat16 *)(Ahi + off) = hi;
+                *(__nv_bfloat16 *)(Alo + off) = lo;
+            }
+        } else {
+            for (int e = gt; e < DP * DP; e += gnt) {
+                int i = e % DP, k = e / DP;
+                Msm[e] = (i < D && k < D) ? (T)(gamma * Ath[(size_t)k * D + i]) : T(0);
+            }
+            grp.sync();
+            for (int i = gt; i < D; i += gnt)
+                for (int e = m.ll_ptr[i]; e < m.ll_ptr[i + 1]; ++e) {
+                    int k = m.ll_col[e];
+                    Msm[k * DP + i] = (T)((double)Msm[k * DP + i] + llv[e] / alpha2);
+                }
+        }
+        // ---- centring terms (MIXED): g = A sbar - b, h = L^T L sbar / alpha^2
         double Lbar = 0.0, Pbar = 0.0;
         if (MIXED) {
             double qa = 0.0, bx = 0.0, pr = 0.0;
@@ -506,198 +684,761 @@ __global__ void __launch_bounds__(256) inner_group_kernel(MeshDev m, InnerArgs a
                     }
                 }
             }
-            if (gt == 0) gint[0] = 0;
-            if (lane < CW) { sj[lane] = 0; sjend[lane] = 0; spar[lane] = -1; }
-            grp.sync();
-            T xc[RT][CTW], x[RT][CTW], p[RT][CTW], acc[RT][CTW];
+            if constexpr (ENG == ENG_MMA) {
+                // ================= warp-MMA engine: S slots per group.
+                // Step layout: warp wl owns m-tiles mt0.. (16 dimensions each) x
+                // n-tiles nt0.. (8 slots each); lane (g, t4) holds rows 16 mt + g and
+                // + 8 of slots 8 nt + 2 t4 and + 1 (the m16n8 accumulator layout).
+                // Chain-start / end-point layout: thread (cs = gt % S, part = gt / S)
+                // handles slot cs on dimensions part, part + NPART, ...
+                constexpr int S = L_::S, NT = S / 8, NTH = 32 * WG, NPART = NTH / S;
+                constexpr int PPW = (DP / 16) * NT / WG;   // (m-tile, n-tile) pairs per warp
+                constexpr int MTW = PPW > NT ? PPW / NT : 1, NTW = PPW / MTW;
+                constexpr int AST = L_::AST, BST = L_::BST, TS = L_::TS, KT = DP / 16;
+                static_assert(MTW * NTW * WG == (DP / 16) * NT, "every (m-tile, n-tile) pair has one owner");
+                const int g = lane >> 2, t4 = lane & 3;
+                const int mt0 = (wl * PPW) / NT, nt0 = (wl * PPW) % NT;
+                const int cs = gt % S, part = gt / S;
+                const __nv_bfloat16 *Ah = (const __nv_bfloat16 *)Ahi, *Al = (const __nv_bfloat16 *)Alo;
+                unsigned *m32 = (unsigned *)masks;   // halves: [0,1] fresh [2,3] active [4,5] blown [6,7] accepted
+                float cov_l[MTW][2], mean_l[MTW][2], cv_l[MTW][2];
+                bool live_l[MTW][2];
 #pragma unroll
-            for (int i = 0; i < RT; ++i)
+                for (int aa = 0; aa < MTW; ++aa)
 #pragma unroll
-                for (int q = 0; q < CTW; ++q) xc[i][q] = T(0);
-            while (true) {
-                // slot refill from the group queue (lane 0), then broadcast
-                if (lane == 0) {
-                    for (int c = 0; c < CW; ++c) {
-                        sfresh[c] = 0;
-                        if (sj[c] >= sjend[c]) {
-                            int qi = atomicAdd(&gint[0], 1);
-                            if (qi < nq) {
-                                int k = keys[qi] & 0xffff;
-                                spar[c] = k;
-                                sj[c] = ids[k];
-                                sjend[c] = ids[k] + cnt[k];
-                                sfresh[c] = 1;
+                    for (int h = 0; h < 2; ++h) {
+                        const int r = 16 * (mt0 + aa) + g + 8 * h;
+                        cov_l[aa][h] = (float)tcov[r];
+                        mean_l[aa][h] = (float)tmean[r];
+                        cv_l[aa][h] = (float)tcv[r];
+                        live_l[aa][h] = r < D;
+                    }
+                float x[MTW][NTW][4], p[MTW][NTW][4], dts[NTW][2];
+                // this warp's rows of M as A fragments (hi, lo): held in registers
+                // for the whole pass when they are few, else loaded every step
+                constexpr bool AREG = MTW * KT <= 4;
+                constexpr int KTR = AREG ? KT : 1;
+                uint32_t fah[MTW][KTR][4], fal[MTW][KTR][4];
+                auto load_a = [&](int kt, int slot) {
+#pragma unroll
+                    for (int aa = 0; aa < MTW; ++aa) {
+                        const int row = 16 * (mt0 + aa) + (lane & 7) + 8 * ((lane >> 3) & 1);
+                        const int col = 16 * kt + 8 * (lane >> 4);
+                        ldsm_x4(fah[aa][slot], Ah + row * AST + col);
+                        ldsm_x4(fal[aa][slot], Al + row * AST + col);
+                    }
+                };
+                if constexpr (AREG) {
+#pragma unroll
+                    for (int kt = 0; kt < KT; ++kt) load_a(kt, kt);
+                }
+                // offsets from the stage mean of the lane's entries -> BF16 hi/lo operand buffer
+                auto write_b = [&](int buf) {
+                    __nv_bfloat16 *bh = (__nv_bfloat16 *)(Bhi + 2 * (size_t)buf * L_::B_BYTES);
+                    __nv_bfloat16 *bl = (__nv_bfloat16 *)(Bhi + (2 * (size_t)buf + 1) * L_::B_BYTES);
+#pragma unroll
+                    for (int aa = 0; aa < MTW; ++aa)
+#pragma unroll
+                        for (int bb = 0; bb < NTW; ++bb)
+#pragma unroll
+                            for (int h = 0; h < 2; ++h) {
+                                const int r = 16 * (mt0 + aa) + g + 8 * h, c0 = 8 * (nt0 + bb) + 2 * t4;
+                                const float d0 = live_l[aa][h] ? x[aa][bb][2 * h] - mean_l[aa][h] : 0.0f;
+                                const float d1 = live_l[aa][h] ? x[aa][bb][2 * h + 1] - mean_l[aa][h] : 0.0f;
+                                const __nv_bfloat162 hi = __floats2bfloat162_rn(d0, d1);
+                                const __nv_bfloat162 lo = __floats2bfloat162_rn(d0 - __low2float(hi), d1 - __high2float(hi));
+                                *(uint32_t *)(bh + r * BST + c0) = bf16x2_bits(hi);
+                                *(uint32_t *)(bl + r * BST + c0) = bf16x2_bits(lo);
                             }
+                };
+                if (gt == 0) gint[0] = 0;
+                if (gt < 2) m32[2 + gt] = 0u;
+                if (gt < S) { sj[gt] = 0; sjend[gt] = 0; spar[gt] = -1; }
+                while (true) {
+                    grp.sync();
+                    // slot refill: thread c < S advances its chain or takes the next parent
+                    if (gt < 64) {
+                        const int c = gt;
+                        bool fresh = false, act = false;
+                        if (c < S) {
+                            if ((m32[2 + (c >> 5)] >> (c & 31)) & 1u) sj[c] += 1;
+                            if (sj[c] >= sjend[c]) {
+                                const int qi = atomicAdd(&gint[0], 1);
+                                if (qi < nq) {
+                                    const int k = keys[qi] & 0xffff;
+                                    spar[c] = k;
+                                    sj[c] = ids[k];
+                                    sjend[c] = ids[k] + cnt[k];
+                                    fresh = true;
+                                    sL[c] = Lc[k];
+                                    sP[c] = Pc[k];
+                                    spost[c] = gamma * Lc[k] + Pc[k];
+                                }
+                            }
+                            act = sj[c] < sjend[c];
+                            sdt[c] = act ? dtau[sj[c]] : 0.0;
+                        }
+                        const unsigned fm = __ballot_sync(FULL, fresh), am = __ballot_sync(FULL, act);
+                        if (lane == 0) { m32[0 + wl] = fm; m32[2 + wl] = am; m32[4 + wl] = 0u; }
+                    }
+                    grp.sync();
+                    const unsigned long long actm = masks[1], frm = masks[0];
+                    if (actm == 0ull) break;
+                    // chain start: parent state of fresh slots (coalesced over
+                    // dimensions), momentum draws and their kinetic energy
+                    if (frm != 0ull)
+                        for (int e = gt; e < S * DP; e += NTH) {
+                            const int c = e / DP, r = e % DP;
+                            if ((frm >> c) & 1ull) tXC[r * TS + c] = r < D ? (float)parts[(size_t)spar[c] * D + r] : 0.0f;
+                        }
+                    double kin = 0.0;
+                    {
+                        const bool on = (actm >> cs) & 1ull;
+                        const int jj = sj[cs];
+                        for (int r = part; r < DP; r += NPART) {
+                            float pv = 0.0f;
+                            if (on && r < D) {
+                                pv = rng_normal_f(a.seed, stream, P_MOM, iter, jj, r) * (float)tisc[r];
+                                kin += (double)(pv * (float)tcov[r] * pv * 0.5f);
+                            }
+                            tP[r * TS + cs] = pv;
                         }
                     }
-                }
-                __syncwarp();
-                bool any = false;
+                    grp.sync();
 #pragma unroll
-                for (int c = 0; c < CW; ++c) any |= sj[c] < sjend[c];
-                if (!any) break;
-                if (lane < CW) {
-                    int c = lane;
-                    if (sfresh[c]) {
-                        int k = spar[c];
-                        sL[c] = Lc[k];
-                        sP[c] = Pc[k];
-                        spost[c] = gamma * Lc[k] + Pc[k];
+                    for (int bb = 0; bb < NTW; ++bb) {
+                        const int c0 = 8 * (nt0 + bb) + 2 * t4;
+                        dts[bb][0] = (float)sdt[c0];
+                        dts[bb][1] = (float)sdt[c0 + 1];
                     }
-                    sdt[c] = sj[c] < sjend[c] ? dtau[sj[c]] : 0.0;
-                    sblown[c] = 0;
+#pragma unroll
+                    for (int aa = 0; aa < MTW; ++aa)
+#pragma unroll
+                        for (int bb = 0; bb < NTW; ++bb)
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                const int r = 16 * (mt0 + aa) + g + 8 * (e >> 1), c = 8 * (nt0 + bb) + 2 * t4 + (e & 1);
+                                x[aa][bb][e] = tXC[r * TS + c];
+                                p[aa][bb][e] = tP[r * TS + c];
+                            }
+                    write_b(0);
+                    // leapfrog (smc_slip.f90:755-904): P/2 (X P)^ntau X/2
+                    int flag = 0;
+                    for (int it = 0; it <= a.ntau; ++it) {
+                        grp.sync();
+                        const unsigned long long blm = masks[2];
+                        const __nv_bfloat16 *bh = (const __nv_bfloat16 *)(Bhi + 2 * (size_t)(it & 1) * L_::B_BYTES);
+                        const __nv_bfloat16 *bl = (const __nv_bfloat16 *)(Bhi + (2 * (size_t)(it & 1) + 1) * L_::B_BYTES);
+                        // all B fragments first (the loads pipeline), then three
+                        // independent accumulation chains: lo*hi, hi*lo, hi*hi
+                        float acc[MTW][NTW][4], acc1[MTW][NTW][4], acc2[MTW][NTW][4];
+#pragma unroll
+                        for (int aa = 0; aa < MTW; ++aa)
+#pragma unroll
+                            for (int bb = 0; bb < NTW; ++bb)
+#pragma unroll
+                                for (int e = 0; e < 4; ++e) acc[aa][bb][e] = acc1[aa][bb][e] = acc2[aa][bb][e] = 0.0f;
+                        constexpr int KTB = (NTW * KT <= 8) ? KT : 1;   // k-tiles of B fragments held at once
+#pragma unroll
+                        for (int k0 = 0; k0 < KT; k0 += KTB) {
+                            uint32_t fbh[KTB][NTW][2], fbl[KTB][NTW][2];
+#pragma unroll
+                            for (int kk = 0; kk < KTB; ++kk)
+#pragma unroll
+                                for (int bb = 0; bb < NTW; ++bb) {
+                                    const int krow = 16 * (k0 + kk) + (lane & 7) + 8 * ((lane >> 3) & 1);
+                                    const int ncol = 8 * (nt0 + bb);
+                                    ldsm_x2_t(fbh[kk][bb], bh + krow * BST + ncol);
+                                    ldsm_x2_t(fbl[kk][bb], bl + krow * BST + ncol);
+                                }
+#pragma unroll
+                            for (int kk = 0; kk < KTB; ++kk) {
+                                const int kt = k0 + kk;
+                                if constexpr (!AREG) load_a(kt, 0);
+                                const int ks = AREG ? kt : 0;
+#pragma unroll
+                                for (int aa = 0; aa < MTW; ++aa)
+#pragma unroll
+                                    for (int bb = 0; bb < NTW; ++bb) {
+                                        mma16816(acc1[aa][bb], fal[aa][ks], fbh[kk][bb]);
+                                        mma16816(acc2[aa][bb], fah[aa][ks], fbl[kk][bb]);
+                                        mma16816(acc[aa][bb], fah[aa][ks], fbh[kk][bb]);
+                                    }
+                            }
+                        }
+#pragma unroll
+                        for (int aa = 0; aa < MTW; ++aa)
+#pragma unroll
+                            for (int bb = 0; bb < NTW; ++bb)
+#pragma unroll
+                                for (int e = 0; e < 4; ++e) acc[aa][bb][e] += acc1[aa][bb][e] + acc2[aa][bb][e];
+                        const float hstep = it == 0 ? 0.5f : 1.0f, xstep = it == a.ntau ? 0.5f : 1.0f;
+#pragma unroll
+                        for (int aa = 0; aa < MTW; ++aa)
+#pragma unroll
+                            for (int bb = 0; bb < NTW; ++bb)
+#pragma unroll
+                                for (int e = 0; e < 4; ++e) {
+                                    const int h = e >> 1, c = 8 * (nt0 + bb) + 2 * t4 + (e & 1);
+                                    if (live_l[aa][h] && ((actm >> c) & 1ull) && !((blm >> c) & 1ull)) {
+                                        const float gr = cv_l[aa][h] + acc[aa][bb][e];
+                                        const float dt = dts[bb][e & 1];
+                                        p[aa][bb][e] = p[aa][bb][e] - gr * hstep * dt;
+                                        x[aa][bb][e] = x[aa][bb][e] + cov_l[aa][h] * p[aa][bb][e] * xstep * dt;
+                                        if (fabsf(x[aa][bb][e]) > 1e3f) atomicOr(&masks[2], 1ull << c);
+                                        else reflect_w<float>(x[aa][bb][e], p[aa][bb][e], mx, flag);
+                                    }
+                                }
+                        if (it < a.ntau) {
+                            write_b((it + 1) & 1);
+                        } else {
+                            // end state into the slot-layout tiles; offsets into the idle B buffer
+                            float *dl = (float *)(Bhi + 2 * (size_t)((it + 1) & 1) * L_::B_BYTES);
+#pragma unroll
+                            for (int aa = 0; aa < MTW; ++aa)
+#pragma unroll
+                                for (int bb = 0; bb < NTW; ++bb)
+#pragma unroll
+                                    for (int e = 0; e < 4; ++e) {
+                                        const int h = e >> 1;
+                                        const int r = 16 * (mt0 + aa) + g + 8 * h, c = 8 * (nt0 + bb) + 2 * t4 + (e & 1);
+                                        tX[r * TS + c] = x[aa][bb][e];
+                                        tP[r * TS + c] = p[aa][bb][e];
+                                        dl[r * TS + c] = live_l[aa][h] ? x[aa][bb][e] - mean_l[aa][h] : 0.0f;
+                                    }
+                        }
+                    }
+                    status |= flag;
+                    grp.sync();
+                    // end point in the slot layout: likelihood and prior offsets,
+                    // kinetic energy, tuning distance (partial over this thread's dimensions)
+                    const unsigned long long blm = masks[2];
+                    const float *dl = (const float *)(Bhi + 2 * (size_t)((a.ntau + 1) & 1) * L_::B_BYTES);
+                    double q0 = 0.0, q1 = 0.0, q2 = 0.0, q3 = 0.0;
+                    if ((actm >> cs) & 1ull) {
+                        // rows part + i NPART of A times the offsets: RPT independent chains
+                        constexpr int RPT = DP / NPART;
+                        float af[RPT];
+#pragma unroll
+                        for (int i = 0; i < RPT; ++i) af[i] = 0.0f;
+                        for (int k = 0; k < D; ++k) {
+                            const float dk = dl[k * TS + cs];
+                            const float *ak = tA32 + k * DP + part;
+#pragma unroll
+                            for (int i = 0; i < RPT; ++i) af[i] = fmaf(ak[i * NPART], dk, af[i]);
+                        }
+#pragma unroll
+                        for (int i = 0; i < RPT; ++i) {
+                            const int r = part + i * NPART;
+                            if (r >= D) continue;
+                            const double ic = 1.0 / vcov[r];
+                            const double del = (double)tX[r * TS + cs] - vmean[r];
+                            q0 += vg[r] * del + 0.5 * (double)dl[r * TS + cs] * (double)af[i];
+                            q1 += vh[r] * del;
+                            const double pr = (double)tP[r * TS + cs];
+                            q2 += 0.5 * pr * vcov[r] * pr;
+                            const double dx = (double)tX[r * TS + cs] - (double)tXC[r * TS + cs];
+                            q3 += dx * dx * ic;
+                        }
+                        const double i2a = 1.0 / (2.0 * alpha2);
+                        for (int r2 = part; r2 < m.nrow; r2 += NPART) {
+                            int cl[9];
+                            double lw[9];
+#pragma unroll
+                            for (int k9 = 0; k9 < 9; ++k9) {
+                                cl[k9] = __ldg(m.l_col + r2 * 9 + k9);
+                                lw[k9] = __ldg(lv + (size_t)r2 * 9 + k9);
+                            }
+                            double tt = 0.0;
+#pragma unroll
+                            for (int k9 = 0; k9 < 9; ++k9)
+                                if (cl[k9] >= 0) tt += lw[k9] * (double)dl[cl[k9] * TS + cs];
+                            q1 += tt * tt * i2a;
+                        }
+                    }
+                    red[0 * NTH + part * S + cs] = q0;
+                    red[1 * NTH + part * S + cs] = q1;
+                    red[2 * NTH + part * S + cs] = q2;
+                    red[3 * NTH + part * S + cs] = q3;
+                    red[4 * NTH + part * S + cs] = kin;
+                    grp.sync();
+                    // Metropolis test and bookkeeping (smc_slip.f90:695-716, 1057-1094)
+                    if (gt < 64) {
+                        const int c = gt;
+                        bool accd = false;
+                        if (c < S && ((actm >> c) & 1ull)) {
+                            double q5[5];
+#pragma unroll
+                            for (int q = 0; q < 5; ++q) {
+                                double tt = 0.0;
+                                for (int pt = 0; pt < NPART; ++pt) tt += red[q * NTH + pt * S + c];
+                                q5[q] = tt;
+                            }
+                            const int jj = sj[c];
+                            const bool blown = (blm >> c) & 1ull;
+                            const double Lx = q5[0] + Lbar, Px = q5[1] + Pbar;
+                            const double post = gamma * Lx + Px;
+                            const double ham = blown ? 1e20 : post + q5[2];
+                            const double dham = (spost[c] + q5[4]) - ham;
+                            if (tuning) score[jj] = blown ? 0.0 : q5[3] * exp(fmin(0.0, dham));
+                            const double u = rng_uniform(a.seed, stream, P_MH, iter, jj, 0);
+                            if (!blown && dham > log(u)) {
+                                accd = true;
+                                sL[c] = Lx;
+                                sP[c] = Px;
+                                spost[c] = post;
+                            }
+                            if (!tuning) {
+                                Ln[jj] = sL[c];
+                                Pn[jj] = sP[c];
+                            }
+                        }
+                        const unsigned am = __ballot_sync(FULL, accd);
+                        if (lane == 0) m32[6 + wl] = am;
+                    }
+                    grp.sync();
+                    const unsigned long long accm = masks[3];
+                    if ((accm >> cs) & 1ull)
+                        for (int r = part; r < DP; r += NPART) tXC[r * TS + cs] = tX[r * TS + cs];
+                    grp.sync();
+                    if (!tuning)
+                        for (int e = gt; e < S * DP; e += NTH) {
+                            const int c = e / DP, r = e % DP;
+                            if (r < D && ((actm >> c) & 1ull)) pnew[(size_t)sj[c] * D + r] = (double)tXC[r * TS + c];
+                        }
                 }
-                __syncwarp();
-                double kin[CTW];
-                T dts[CTW];
-                bool act[CTW];
+                grp.sync();
+            } else if constexpr (TC) {
+                // ================= tcgen05 engine: S slots per group, thread
+                // (row t) owns dimension r = t % DP of slots s0 .. s0+15
+                constexpr int S = L_::S, SPT = 16;
+                const int r = gt % DP, s0 = (gt / DP) * SPT;
+                const bool rowlive = r < D;
+                const float cov_r = (float)tcov[r], mean_r = (float)tmean[r], cv_r = (float)tcv[r];
+                const float isc_r = (float)tisc[r];
+                const double vcov_r = vcov[r], vmean_r = vmean[r], vg_r = vg[r], vh_r = vh[r];
+                const uint32_t tcol = tmem_base + (uint32_t)(grp.id * S);
+                const uint32_t taddr = tcol + ((uint32_t)(32 * wl) << 16) + (uint32_t)s0;
+                const uint32_t idesc = tc::idesc_bf16_f32(128, S);
+                const uint32_t sa_hi = tc::smem_u32(Ahi), sa_lo = tc::smem_u32(Alo);
+                const uint32_t sb_hi = tc::smem_u32(Bhi), sb_lo = tc::smem_u32(Blo);
+                unsigned *m32 = (unsigned *)masks;   // halves: [0,1] fresh [2,3] active [4,5] blown [6,7] accepted
+                float xc[SPT], x[SPT], p[SPT], kin[SPT], dts[SPT];
 #pragma unroll
-                for (int q = 0; q < CTW; ++q) {
-                    int c = cg * CTW + q;
-                    act[q] = sj[c] < sjend[c];
-                    dts[q] = (T)sdt[c];
-                    kin[q] = 0.0;
-                    const int jj = sj[c];
+                for (int s = 0; s < SPT; ++s) xc[s] = 0.0f;
+                if (gt == 0) gint[0] = 0;
+                if (gt < 2) m32[2 + gt] = 0u;
+                if (gt < S) { sj[gt] = 0; sjend[gt] = 0; spar[gt] = -1; }
+                bool failed = false;
+                while (true) {
+                    grp.sync();
+                    // slot refill: thread c < S advances its chain or takes the next parent
+                    if (gt < 64) {
+                        const int c = gt;
+                        bool fresh = false, act = false;
+                        if (c < S) {
+                            if ((m32[2 + (c >> 5)] >> (c & 31)) & 1u) sj[c] += 1;
+                            if (sj[c] >= sjend[c]) {
+                                const int qi = atomicAdd(&gint[0], 1);
+                                if (qi < nq) {
+                                    const int k = keys[qi] & 0xffff;
+                                    spar[c] = k;
+                                    sj[c] = ids[k];
+                                    sjend[c] = ids[k] + cnt[k];
+                                    fresh = true;
+                                    sL[c] = Lc[k];
+                                    sP[c] = Pc[k];
+                                    spost[c] = gamma * Lc[k] + Pc[k];
+                                }
+                            }
+                            act = sj[c] < sjend[c];
+                            sdt[c] = act ? dtau[sj[c]] : 0.0;
+                        }
+                        const unsigned fm = __ballot_sync(FULL, fresh), am = __ballot_sync(FULL, act);
+                        if (lane == 0) { m32[0 + wl] = fm; m32[2 + wl] = am; m32[4 + wl] = 0u; }
+                    }
+                    grp.sync();
+                    const unsigned long long actm = masks[1], frm = masks[0];
+                    if (actm == 0ull) break;
+                    // chain start: parent state, momentum draw, first operand tile
 #pragma unroll
-                    for (int i = 0; i < RT; ++i) {
-                        int r = rg * RT + i;
-                        if (sfresh[c]) xc[i][q] = (act[q] && r < D) ? (T)parts[(size_t)spar[c] * D + r] : T(0);
-                        T pv = T(0);
-                        if (act[q] && r < D) {
-                            if (MIXED) {
-                                pv = rng_normal_f(a.seed, stream, P_MOM, iter, jj, r) * tisc[r];
-                                kin[q] += (double)(pv * tcov[r] * pv * T(0.5));
+                    for (int s = 0; s < SPT; ++s) {
+                        const int c = s0 + s;
+                        const bool on = rowlive && ((actm >> c) & 1ull);
+                        if ((frm >> c) & 1ull) xc[s] = on ? (float)parts[(size_t)spar[c] * D + r] : 0.0f;
+                        dts[s] = (float)sdt[c];
+                        float pv = 0.0f;
+                        if (on) pv = rng_normal_f(a.seed, stream, P_MOM, iter, sj[c], r) * isc_r;
+                        kin[s] = pv * cov_r * pv * 0.5f;
+                        p[s] = pv;
+                        x[s] = xc[s];
+                        __nv_bfloat16 hi, lo;
+                        tc::split_bf16(rowlive ? x[s] - mean_r : 0.0f, hi, lo);
+                        const uint32_t off = tc::core_offset(c, r, L_::LBO_B);
+                        *(__nv_bfloat16 *)(Bhi + off) = hi;
+                        *(__nv_bfloat16 *)(Blo + off) = lo;
+                    }
+                    // leapfrog (smc_slip.f90:755-904): P/2 (X P)^ntau X/2
+                    int flag = 0;
+                    for (int it = 0; it <= a.ntau; ++it) {
+                        tc::fence_async_smem();
+                        tc::fence_before_sync();
+                        grp.sync();
+                        if (gint[3]) { failed = true; break; }
+                        const unsigned long long blm = masks[2];
+                        if (gt == 0) {
+                            tc::fence_after_sync();
+#pragma unroll
+                            for (int kk = 0; kk < DP / 16; ++kk) {
+                                const uint64_t ah = tc::smem_desc(sa_hi + kk * 2 * L_::LBO_A, L_::LBO_A, 128);
+                                const uint64_t al = tc::smem_desc(sa_lo + kk * 2 * L_::LBO_A, L_::LBO_A, 128);
+                                const uint64_t bh = tc::smem_desc(sb_hi + kk * 2 * L_::LBO_B, L_::LBO_B, 128);
+                                const uint64_t bl = tc::smem_desc(sb_lo + kk * 2 * L_::LBO_B, L_::LBO_B, 128);
+                                tc::mma_bf16(tcol, ah, bh, idesc, kk > 0 ? 1u : 0u);
+                                tc::mma_bf16(tcol, ah, bl, idesc, 1u);
+                                tc::mma_bf16(tcol, al, bh, idesc, 1u);
+                            }
+                            tc::mma_commit(mbar);
+                        }
+                        if (!tc::mbar_wait(mbar, phase, WAIT_TRIES)) gint[3] = 1;
+                        phase ^= 1u;
+                        tc::fence_after_sync();
+                        float acc[SPT];
+                        tc::tmem_ld16(taddr, acc);
+                        tc::tmem_wait_ld();
+                        const float hstep = it == 0 ? 0.5f : 1.0f, xstep = it == a.ntau ? 0.5f : 1.0f;
+#pragma unroll
+                        for (int s = 0; s < SPT; ++s) {
+                            const int c = s0 + s;
+                            if (rowlive && ((actm >> c) & 1ull) && !((blm >> c) & 1ull)) {
+                                const float gr = cv_r + acc[s];
+                                p[s] = p[s] - gr * hstep * dts[s];
+                                x[s] = x[s] + cov_r * p[s] * xstep * dts[s];
+                                if (fabsf(x[s]) > 1e3f) atomicOr(&masks[2], 1ull << c);
+                                else reflect_w<float>(x[s], p[s], mx, flag);
+                            }
+                            const float dl = rowlive ? x[s] - mean_r : 0.0f;
+                            if (it < a.ntau) {
+                                __nv_bfloat16 hi, lo;
+                                tc::split_bf16(dl, hi, lo);
+                                const uint32_t off = tc::core_offset(c, r, L_::LBO_B);
+                                *(__nv_bfloat16 *)(Bhi + off) = hi;
+                                *(__nv_bfloat16 *)(Blo + off) = lo;
                             } else {
-                                pv = (T)(rng_normal(a.seed, stream, P_MOM, iter, jj, r) / sqrt(vcov[r]));
-                                kin[q] += (double)pv * vcov[r] * (double)pv / 2.0;
+                                Xf[r * S + c] = dl;
                             }
                         }
-                        p[i][q] = pv;
-                        x[i][q] = xc[i][q];
-                        Xw0[r * CW + c] = (r < D) ? (MIXED ? x[i][q] - tmean[r] : x[i][q]) : T(0);
                     }
-                    kin[q] = hsum(kin[q]);
-                }
-                if (rg == 0) {
+                    status |= flag;
+                    if (failed) break;
+                    grp.sync();
+                    // end point: per-slot sums over dimensions of the likelihood and
+                    // prior offsets, kinetic energies and the tuning distance
+                    const unsigned long long blm = masks[2];
+                    const int wib = r >> 5;
+                    double v[SPT];
+                    {
+                        float af[SPT];
 #pragma unroll
-                    for (int q = 0; q < CTW; ++q) sham[cg * CTW + q] = spost[cg * CTW + q] + kin[q];
-                }
-                __syncwarp();
-                // leapfrog (smc_slip.f90:755-904): P/2 (X P)^ntau X/2
-                int flag = 0;
-                for (int it = 0; it <= a.ntau; ++it) {
-                    T *Xr = (it & 1) ? Xw1 : Xw0;
-                    T *Xw = (it & 1) ? Xw0 : Xw1;
-                    warp_gemm<T, RT>(Msm, Xr, rg, cg, acc);
-                    const T hstep = (it == 0) ? T(0.5) : T(1);
-                    const T xstep = (it == a.ntau) ? T(0.5) : T(1);
+                        for (int s = 0; s < SPT; ++s) af[s] = 0.0f;
+                        if (rowlive)
+                            for (int k = 0; k < D; ++k) {
+                                const float ak = A32[(size_t)k * D + r];
+                                const float *xk = Xf + k * S + s0;
 #pragma unroll
-                    for (int q = 0; q < CTW; ++q) {
-                        int c = cg * CTW + q;
-                        bool live = act[q] && !sblown[c];
-#pragma unroll
-                        for (int i = 0; i < RT; ++i) {
-                            int r = rg * RT + i;
-                            if (live && r < D) {
-                                T gr = MIXED ? tcv[r] + acc[i][q] : acc[i][q] - tcv[r];
-                                p[i][q] = p[i][q] - gr * hstep * dts[q];
-                                x[i][q] = x[i][q] + tcov[r] * p[i][q] * xstep * dts[q];
-                                if (fabs(x[i][q]) > T(1e3)) atomicOr(&sblown[c], 1);
-                                else reflect_w<T>(x[i][q], p[i][q], mx, flag);
+                                for (int s = 0; s < SPT; ++s) af[s] = fmaf(ak, xk[s], af[s]);
                             }
-                            Xw[r * CW + c] = (r < D) ? (MIXED ? x[i][q] - tmean[r] : x[i][q]) : T(0);
+#pragma unroll
+                        for (int s = 0; s < SPT; ++s) {
+                            const double del = (double)x[s] - vmean_r;
+                            v[s] = rowlive ? vg_r * del + 0.5 * (double)Xf[r * S + s0 + s] * (double)af[s] : 0.0;
+                        }
+                        const double t = wreduce16(v, lane);
+                        if (!(lane & 1)) red[0 * 64 + wib * S + s0 + (lane >> 1)] = t;
+                    }
+                    {
+#pragma unroll
+                        for (int s = 0; s < SPT; ++s) v[s] = rowlive ? vh_r * ((double)x[s] - vmean_r) : 0.0;
+                        for (int r2 = r; r2 < m.nrow; r2 += DP) {
+                            double t[SPT];
+#pragma unroll
+                            for (int s = 0; s < SPT; ++s) t[s] = 0.0;
+                            for (int k9 = 0; k9 < 9; ++k9) {
+                                const int cl = m.l_col[r2 * 9 + k9];
+                                if (cl < 0) continue;
+                                const double lvv = lv[(size_t)r2 * 9 + k9];
+                                const float *xk = Xf + cl * S + s0;
+#pragma unroll
+                                for (int s = 0; s < SPT; ++s) t[s] += lvv * (double)xk[s];
+                            }
+#pragma unroll
+                            for (int s = 0; s < SPT; ++s) v[s] += t[s] * t[s] / (2.0 * alpha2);
+                        }
+                        const double t = wreduce16(v, lane);
+                        if (!(lane & 1)) red[1 * 64 + wib * S + s0 + (lane >> 1)] = t;
+                    }
+                    {
+#pragma unroll
+                        for (int s = 0; s < SPT; ++s) v[s] = rowlive ? (double)p[s] * vcov_r * (double)p[s] / 2.0 : 0.0;
+                        const double t = wreduce16(v, lane);
+                        if (!(lane & 1)) red[2 * 64 + wib * S + s0 + (lane >> 1)] = t;
+                    }
+                    {
+#pragma unroll
+                        for (int s = 0; s < SPT; ++s) {
+                            const double dx = (double)x[s] - (double)xc[s];
+                            v[s] = rowlive ? dx * dx / vcov_r : 0.0;
+                        }
+                        const double t = wreduce16(v, lane);
+                        if (!(lane & 1)) red[3 * 64 + wib * S + s0 + (lane >> 1)] = t;
+                    }
+                    {
+#pragma unroll
+                        for (int s = 0; s < SPT; ++s) v[s] = (double)kin[s];
+                        const double t = wreduce16(v, lane);
+                        if (!(lane & 1)) red[4 * 64 + wib * S + s0 + (lane >> 1)] = t;
+                    }
+                    grp.sync();
+                    // Metropolis test and bookkeeping (smc_slip.f90:695-716, 1057-1094)
+                    if (gt < 64) {
+                        const int c = gt;
+                        bool accd = false;
+                        if (c < S && ((actm >> c) & 1ull)) {
+                            double q5[5];
+#pragma unroll
+                            for (int q = 0; q < 5; ++q) {
+                                double t = 0.0;
+                                for (int wb = 0; wb < DP / 32; ++wb) t += red[q * 64 + wb * S + c];
+                                q5[q] = t;
+                            }
+                            const int jj = sj[c];
+                            const bool blown = (blm >> c) & 1ull;
+                            const double Lx = q5[0] + Lbar, Px = q5[1] + Pbar;
+                            const double post = gamma * Lx + Px;
+                            const double ham = blown ? 1e20 : post + q5[2];
+                            const double dham = (spost[c] + q5[4]) - ham;
+                            if (tuning) score[jj] = blown ? 0.0 : q5[3] * exp(fmin(0.0, dham));
+                            const double u = rng_uniform(a.seed, stream, P_MH, iter, jj, 0);
+                            if (!blown && dham > log(u)) {
+                                accd = true;
+                                sL[c] = Lx;
+                                sP[c] = Px;
+                                spost[c] = post;
+                            }
+                            if (!tuning) {
+                                Ln[jj] = sL[c];
+                                Pn[jj] = sP[c];
+                            }
+                        }
+                        const unsigned am = __ballot_sync(FULL, accd);
+                        if (lane == 0) m32[6 + wl] = am;
+                    }
+                    grp.sync();
+                    const unsigned long long accm = masks[3];
+#pragma unroll
+                    for (int s = 0; s < SPT; ++s) {
+                        const int c = s0 + s;
+                        if ((accm >> c) & 1ull) xc[s] = x[s];
+                        if (!tuning && rowlive && ((actm >> c) & 1ull)) pnew[(size_t)sj[c] * D + r] = (double)xc[s];
+                    }
+                }
+                grp.sync();
+                if (gint[3]) break;
+            } else {
+                // ================= CUDA-core engine: 8 slots per warp
+                if (gt == 0) gint[0] = 0;
+                if (lane < CW) { sj[lane] = 0; sjend[lane] = 0; spar[lane] = -1; }
+                grp.sync();
+                T xc[RT][CTW], x[RT][CTW], p[RT][CTW], acc[RT][CTW];
+#pragma unroll
+                for (int i = 0; i < RT; ++i)
+#pragma unroll
+                    for (int q = 0; q < CTW; ++q) xc[i][q] = T(0);
+                while (true) {
+                    // slot refill from the group queue (lane 0), then broadcast
+                    if (lane == 0) {
+                        for (int c = 0; c < CW; ++c) {
+                            sfresh[c] = 0;
+                            if (sj[c] >= sjend[c]) {
+                                int qi = atomicAdd(&gint[0], 1);
+                                if (qi < nq) {
+                                    int k = keys[qi] & 0xffff;
+                                    spar[c] = k;
+                                    sj[c] = ids[k];
+                                    sjend[c] = ids[k] + cnt[k];
+                                    sfresh[c] = 1;
+                                }
+                            }
                         }
                     }
                     __syncwarp();
-                }
-                status |= flag;
-                // end point: likelihood, prior, kinetic energy, tuning score
-                T *Xf = ((a.ntau + 1) & 1) ? Xw1 : Xw0;
-                double pl[CTW], pk[CTW], psc[CTW], pp[CTW];
+                    bool any = false;
 #pragma unroll
-                for (int q = 0; q < CTW; ++q) {
-                    int c = cg * CTW + q;
-                    pl[q] = pk[q] = psc[q] = pp[q] = 0.0;
+                    for (int c = 0; c < CW; ++c) any |= sj[c] < sjend[c];
+                    if (!any) break;
+                    if (lane < CW) {
+                        int c = lane;
+                        if (sfresh[c]) {
+                            int k = spar[c];
+                            sL[c] = Lc[k];
+                            sP[c] = Pc[k];
+                            spost[c] = gamma * Lc[k] + Pc[k];
+                        }
+                        sdt[c] = sj[c] < sjend[c] ? dtau[sj[c]] : 0.0;
+                        sblown[c] = 0;
+                    }
+                    __syncwarp();
+                    double kin[CTW];
+                    T dts[CTW];
+                    bool act[CTW];
 #pragma unroll
-                    for (int i = 0; i < RT; ++i) {
-                        int r = rg * RT + i;
-                        if (r >= D) continue;
-                        double ar = 0.0;
-                        if (MIXED) {
-                            float af = 0.0f;
-                            for (int k = 0; k < D; ++k) af = fmaf(A32[(size_t)k * D + r], (float)Xf[k * CW + c], af);
-                            ar = (double)af;
-                            double del = (double)x[i][q] - vmean[r];
-                            pl[q] += vg[r] * del + 0.5 * (double)Xf[r * CW + c] * ar;
-                            pp[q] += vh[r] * del;
-                        } else {
-                            for (int k = 0; k < D; ++k) ar += Ath[(size_t)k * D + r] * (double)Xf[k * CW + c];
-                            double xv = (double)x[i][q];
-                            pl[q] += xv * ar - 2.0 * vb[r] * xv;
+                    for (int q = 0; q < CTW; ++q) {
+                        int c = cg * CTW + q;
+                        act[q] = sj[c] < sjend[c];
+                        dts[q] = (T)sdt[c];
+                        kin[q] = 0.0;
+                        const int jj = sj[c];
+#pragma unroll
+                        for (int i = 0; i < RT; ++i) {
+                            int r = rg * RT + i;
+                            if (sfresh[c]) xc[i][q] = (act[q] && r < D) ? (T)parts[(size_t)spar[c] * D + r] : T(0);
+                            T pv = T(0);
+                            if (act[q] && r < D) {
+                                if (MIXED) {
+                                    pv = rng_normal_f(a.seed, stream, P_MOM, iter, jj, r) * tisc[r];
+                                    kin[q] += (double)(pv * tcov[r] * pv * T(0.5));
+                                } else {
+                                    pv = (T)(rng_normal(a.seed, stream, P_MOM, iter, jj, r) / sqrt(vcov[r]));
+                                    kin[q] += (double)pv * vcov[r] * (double)pv / 2.0;
+                                }
+                            }
+                            p[i][q] = pv;
+                            x[i][q] = xc[i][q];
+                            Xw0[r * CW + c] = (r < D) ? (MIXED ? x[i][q] - tmean[r] : x[i][q]) : T(0);
                         }
-                        pk[q] += (double)p[i][q] * vcov[r] * (double)p[i][q] / 2.0;
-                        double dx = (double)x[i][q] - (double)xc[i][q];
-                        psc[q] += dx * dx / vcov[r];
+                        kin[q] = hsum(kin[q]);
                     }
-                    for (int r = rg; r < m.nrow; r += RGW) {
-                        double t = 0.0;
-                        for (int k9 = 0; k9 < 9; ++k9) {
-                            int cl = m.l_col[r * 9 + k9];
-                            if (cl >= 0) t += lv[(size_t)r * 9 + k9] * (double)Xf[cl * CW + c];
+                    if (rg == 0) {
+#pragma unroll
+                        for (int q = 0; q < CTW; ++q) sham[cg * CTW + q] = spost[cg * CTW + q] + kin[q];
+                    }
+                    __syncwarp();
+                    // leapfrog (smc_slip.f90:755-904): P/2 (X P)^ntau X/2
+                    int flag = 0;
+                    for (int it = 0; it <= a.ntau; ++it) {
+                        T *Xr = (it & 1) ? Xw1 : Xw0;
+                        T *Xw = (it & 1) ? Xw0 : Xw1;
+                        warp_gemm<T, RT>(Msm, Xr, rg, cg, acc);
+                        const T hstep = (it == 0) ? T(0.5) : T(1);
+                        const T xstep = (it == a.ntau) ? T(0.5) : T(1);
+#pragma unroll
+                        for (int q = 0; q < CTW; ++q) {
+                            int c = cg * CTW + q;
+                            bool live = act[q] && !sblown[c];
+#pragma unroll
+                            for (int i = 0; i < RT; ++i) {
+                                int r = rg * RT + i;
+                                if (live && r < D) {
+                                    T gr = MIXED ? tcv[r] + acc[i][q] : acc[i][q] - tcv[r];
+                                    p[i][q] = p[i][q] - gr * hstep * dts[q];
+                                    x[i][q] = x[i][q] + tcov[r] * p[i][q] * xstep * dts[q];
+                                    if (fabs(x[i][q]) > T(1e3)) atomicOr(&sblown[c], 1);
+                                    else reflect_w<T>(x[i][q], p[i][q], mx, flag);
+                                }
+                                Xw[r * CW + c] = (r < D) ? (MIXED ? x[i][q] - tmean[r] : x[i][q]) : T(0);
+                            }
                         }
-                        pp[q] += t * t / (2.0 * alpha2);
+                        __syncwarp();
                     }
-                    pl[q] = hsum(pl[q]);
-                    pk[q] = hsum(pk[q]);
-                    psc[q] = hsum(psc[q]);
-                    pp[q] = hsum(pp[q]);
-                }
-                // Metropolis test and bookkeeping (smc_slip.f90:695-716, 1057-1094)
-                int accm = 0;
-                if (rg == 0) {
+                    status |= flag;
+                    // end point: likelihood, prior, kinetic energy, tuning score
+                    T *Xf = ((a.ntau + 1) & 1) ? Xw1 : Xw0;
+                    double pl[CTW], pk[CTW], psc[CTW], pp[CTW];
+#pragma unroll
+                    for (int q = 0; q < CTW; ++q) {
+                        int c = cg * CTW + q;
+                        pl[q] = pk[q] = psc[q] = pp[q] = 0.0;
+#pragma unroll
+                        for (int i = 0; i < RT; ++i) {
+                            int r = rg * RT + i;
+                            if (r >= D) continue;
+                            double ar = 0.0;
+                            if (MIXED) {
+                                float af = 0.0f;
+                                for (int k = 0; k < D; ++k) af = fmaf(A32[(size_t)k * D + r], (float)Xf[k * CW + c], af);
+                                ar = (double)af;
+                                double del = (double)x[i][q] - vmean[r];
+                                pl[q] += vg[r] * del + 0.5 * (double)Xf[r * CW + c] * ar;
+                                pp[q] += vh[r] * del;
+                            } else {
+                                for (int k = 0; k < D; ++k) ar += Ath[(size_t)k * D + r] * (double)Xf[k * CW + c];
+                                double xv = (double)x[i][q];
+                                pl[q] += xv * ar - 2.0 * vb[r] * xv;
+                            }
+                            pk[q] += (double)p[i][q] * vcov[r] * (double)p[i][q] / 2.0;
+                            double dx = (double)x[i][q] - (double)xc[i][q];
+                            psc[q] += dx * dx / vcov[r];
+                        }
+                        for (int r = rg; r < m.nrow; r += RGW) {
+                            double t = 0.0;
+                            for (int k9 = 0; k9 < 9; ++k9) {
+                                int cl = m.l_col[r * 9 + k9];
+                                if (cl >= 0) t += lv[(size_t)r * 9 + k9] * (double)Xf[cl * CW + c];
+                            }
+                            pp[q] += t * t / (2.0 * alpha2);
+                        }
+                        pl[q] = hsum(pl[q]);
+                        pk[q] = hsum(pk[q]);
+                        psc[q] = hsum(psc[q]);
+                        pp[q] = hsum(pp[q]);
+                    }
+                    // Metropolis test and bookkeeping (smc_slip.f90:695-716, 1057-1094)
+                    int accm = 0;
+                    if (rg == 0) {
+#pragma unroll
+                        for (int q = 0; q < CTW; ++q) {
+                            int c = cg * CTW + q;
+                            if (!act[q]) continue;
+                            int jj = sj[c];
+                            bool blown = sblown[c];
+                            double Lx = MIXED ? pl[q] + Lbar : (pl[q] + dsd) / 2.0 + lconst;
+                            double Px = MIXED ? pp[q] + Pbar : pp[q];
+                            double post = gamma * Lx + Px;
+                            double ham = blown ? 1e20 : post + pk[q];
+                            double dham = sham[c] - ham;
+                            if (tuning) score[jj] = blown ? 0.0 : psc[q] * exp(fmin(0.0, dham));
+                            double u = rng_uniform(a.seed, stream, P_MH, iter, jj, 0);
+                            if (!blown && dham > log(u)) {
+                                accm |= 1 << q;
+                                sL[c] = Lx;
+                                sP[c] = Px;
+                                spost[c] = post;
+                            }
+                            if (!tuning) {
+                                Ln[jj] = sL[c];
+                                Pn[jj] = sP[c];
+                            }
+                        }
+                    }
+                    accm = __shfl_sync(FULL, accm, lane & 16);
 #pragma unroll
                     for (int q = 0; q < CTW; ++q) {
                         int c = cg * CTW + q;
                         if (!act[q]) continue;
-                        int jj = sj[c];
-                        bool blown = sblown[c];
-                        double Lx = MIXED ? pl[q] + Lbar : (pl[q] + dsd) / 2.0 + lconst;
-                        double Px = MIXED ? pp[q] + Pbar : pp[q];
-                        double post = gamma * Lx + Px;
-                        double ham = blown ? 1e20 : post + pk[q];
-                        double dham = sham[c] - ham;
-                        if (tuning) score[jj] = blown ? 0.0 : psc[q] * exp(fmin(0.0, dham));
-                        double u = rng_uniform(a.seed, stream, P_MH, iter, jj, 0);
-                        if (!blown && dham > log(u)) {
-                            accm |= 1 << q;
-                            sL[c] = Lx;
-                            sP[c] = Px;
-                            spost[c] = post;
-                        }
-                        if (!tuning) {
-                            Ln[jj] = sL[c];
-                            Pn[jj] = sP[c];
+                        bool accd = (accm >> q) & 1;
+#pragma unroll
+                        for (int i = 0; i < RT; ++i) {
+                            int r = rg * RT + i;
+                            if (accd) xc[i][q] = x[i][q];
+                            if (!tuning && r < D) pnew[(size_t)sj[c] * D + r] = (double)xc[i][q];
                         }
                     }
+                    __syncwarp();
+                    if (lane < CW && sj[lane] < sjend[lane]) sj[lane] += 1;
+                    __syncwarp();
                 }
-                accm = __shfl_sync(FULL, accm, lane & 16);
-#pragma unroll
-                for (int q = 0; q < CTW; ++q) {
-                    int c = cg * CTW + q;
-                    if (!act[q]) continue;
-                    bool accd = (accm >> q) & 1;
-#pragma unroll
-                    for (int i = 0; i < RT; ++i) {
-                        int r = rg * RT + i;
-                        if (accd) xc[i][q] = x[i][q];
-                        if (!tuning && r < D) pnew[(size_t)sj[c] * D + r] = (double)xc[i][q];
-                    }
-                }
-                __syncwarp();
-                if (lane < CW && sj[lane] < sjend[lane]) sj[lane] += 1;
-                __syncwarp();
+                grp.sync();
             }
-            grp.sync();
             if (tuning) {
                 // tuned children in ascending order, then step sizes resampled by score (warp 0)
                 for (int q = gt; q < nq; q += gnt) {
@@ -761,10 +1502,21 @@ __global__ void __launch_bounds__(256) inner_group_kernel(MeshDev m, InnerArgs a
                 grp.sync();
             }
         }
+        if (ENG == ENG_TC && gint[3]) {
+            // a tensor-core completion wait gave up: abandon this evaluation
+            neglog = 1e10;
+            status |= SMCGPU_ST_WAIT_CAP;
+            break;
+        }
         for (size_t e = gt; e < (size_t)N * D; e += gnt) parts[e] = pnew[e];
         for (int k = gt; k < N; k += gnt) { Lc[k] = Ln[k]; Pc[k] = Pn[k]; }
         grp.sync();
         ++iter;
+    }
+    if constexpr (TC) {
+        // an MMA batch whose wait gave up may still be in flight: wait for it
+        // (bounded) before the tensor memory is released
+        if (gt == 0 && gint[3]) tc::mbar_wait(mbar, phase ^ 1u, WAIT_TRIES);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) status |= __shfl_xor_sync(FULL, status, o);
@@ -779,8 +1531,52 @@ __global__ void __launch_bounds__(256) inner_group_kernel(MeshDev m, InnerArgs a
     }
 }
 
+__host__ __device__ constexpr uint32_t tmem_columns(int n) {
+    uint32_t c = 32;
+    while (c < (uint32_t)n) c <<= 1;
+    return c;
+}
+
+template <typename T, int RT, int ENG, int WG>
+__global__ void __launch_bounds__(ENG == ENG_MMA ? 512 : 256) inner_group_kernel(MeshDev m, InnerArgs a, int W, int G) {
+    extern __shared__ __align__(128) unsigned char smem_all[];
+    __shared__ uint32_t tmem_slot;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    Group grp;
+    grp.id = warp / W;
+    grp.W = W;
+    grp.wl = warp % W;
+    grp.lane = lane;
+    grp.gt = grp.wl * 32 + lane;
+    grp.nt = 32 * W;
+    grp.scr = nullptr;
+    uint32_t tmem_base = 0;
+    constexpr uint32_t S = Layout<T, RT, ENG>::S;
+    const uint32_t ncols = tmem_columns(G * (int)S);
+    if constexpr (ENG == ENG_TC) {
+        if (warp == 0) {
+            tc::tmem_alloc(&tmem_slot, ncols);
+            tc::tmem_relinquish();
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        tmem_base = tmem_slot;
+    }
+    const int th = blockIdx.x * G + grp.id;
+    if (grp.id < G && th < a.n_theta)
+        group_body<T, RT, ENG, WG>(m, a, grp, th, smem_all + (size_t)grp.id * Layout<T, RT, ENG>::bytes(W), tmem_base);
+    if constexpr (ENG == ENG_TC) {
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (warp == 0) tc::tmem_dealloc(tmem_base, ncols);
+    }
+}
+
 template <typename T, int RT>
-static cudaError_t launch_group_t(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W) {
+static cudaError_t launch_cc_t(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W) {
+    using L_ = Layout<T, RT, ENG_CC>;
     int dev = 0, maxsm = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -792,19 +1588,42 @@ static cudaError_t launch_group_t(const MeshDev &m, const InnerArgs &a, cudaStre
         W = 1;
         while (W < 8 && (long long)a.n_theta * W * 2 <= slots) W *= 2;
     }
-    size_t per = GroupSmem<T, RT>::bytes(W);
+    size_t per = L_::bytes(W);
     int G = (int)std::min<size_t>((size_t)(8 / W), (size_t)maxsm / per);
     while (G < 1 && W > 1) {
         W /= 2;
-        per = GroupSmem<T, RT>::bytes(W);
+        per = L_::bytes(W);
         G = (int)std::min<size_t>((size_t)(8 / W), (size_t)maxsm / per);
     }
     if (G < 1) return cudaErrorInvalidValue;
     size_t sm = per * G;
-    cudaError_t e = cudaFuncSetAttribute(inner_group_kernel<T, RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(inner_group_kernel<T, RT, ENG_CC, 0>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     unsigned blocks = (unsigned)((a.n_theta + G - 1) / G);
-    inner_group_kernel<T, RT><<<blocks, 32 * W * G, sm, s>>>(m, a, W, G);
+    inner_group_kernel<T, RT, ENG_CC, 0><<<blocks, 32 * W * G, sm, s>>>(m, a, W, G);
+    return cudaGetLastError();
+}
+
+// WG warps per geometry: as many geometries per CTA as shared memory and the
+// register file allow (gmax), but no more than needed to give every SM a CTA
+template <int RT, int ENG, int WG>
+static cudaError_t launch_wg_t(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int gmax) {
+    using L_ = Layout<float, RT, ENG>;
+    int dev = 0, maxsm = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const size_t per = L_::bytes(WG);
+    int G = (int)std::min<size_t>((size_t)gmax, (size_t)maxsm / per);
+    G = std::min(G, std::max(1, (a.n_theta + nsm - 1) / nsm));
+    if (G < 1) return cudaErrorInvalidValue;
+    const size_t sm = per * G;
+    cudaError_t e = cudaFuncSetAttribute(inner_group_kernel<float, RT, ENG, WG>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = (unsigned)((a.n_theta + G - 1) / G);
+    inner_group_kernel<float, RT, ENG, WG><<<blocks, 32 * WG * G, sm, s>>>(m, a, WG, G);
     return cudaGetLastError();
 }
 
@@ -814,16 +1633,30 @@ cudaError_t launch_inner(const MeshDev &m, const InnerArgs &a, cudaStream_t s, c
     const int D = a.D;
     const int W = a.warps_per_theta;
     if (!a.mixed) {
-        if (D <= 32) return launch_group_t<double, 2>(m, a, s, W);
-        if (D <= 64) return launch_group_t<double, 4>(m, a, s, W);
-        if (D <= 96) return launch_group_t<double, 6>(m, a, s, W);
-        if (D <= 128) return launch_group_t<double, 8>(m, a, s, W);
+        if (D <= 32) return launch_cc_t<double, 2>(m, a, s, W);
+        if (D <= 64) return launch_cc_t<double, 4>(m, a, s, W);
+        if (D <= 96) return launch_cc_t<double, 6>(m, a, s, W);
+        if (D <= 128) return launch_cc_t<double, 8>(m, a, s, W);
+    } else if (a.engine == SMCGPU_ENGINE_MMA && D <= 128) {
+        // 16 warps per geometry while the batch leaves SMs free (lowest
+        // latency per geometry), 8 warps and two geometries per CTA beyond
+        int nsm = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        const bool wide = a.n_theta <= nsm;
+        if (D <= 32) return wide ? launch_wg_t<2, ENG_MMA, 16>(m, a, s, 1) : launch_wg_t<2, ENG_MMA, 8>(m, a, s, 2);
+        if (D <= 64) return wide ? launch_wg_t<4, ENG_MMA, 16>(m, a, s, 1) : launch_wg_t<4, ENG_MMA, 8>(m, a, s, 2);
+        return wide ? launch_wg_t<8, ENG_MMA, 16>(m, a, s, 1) : launch_wg_t<8, ENG_MMA, 8>(m, a, s, 2);
+    } else if (a.engine == SMCGPU_ENGINE_TCGEN05 && D <= 128) {
+        if (D <= 32) return launch_wg_t<2, ENG_TC, 4>(m, a, s, 2);
+        if (D <= 64) return launch_wg_t<4, ENG_TC, 4>(m, a, s, 2);
+        return launch_wg_t<8, ENG_TC, 4>(m, a, s, 2);
     } else {
-        if (D <= 32) return launch_group_t<float, 2>(m, a, s, W);
-        if (D <= 64) return launch_group_t<float, 4>(m, a, s, W);
-        if (D <= 96) return launch_group_t<float, 6>(m, a, s, W);
-        if (D <= 128) return launch_group_t<float, 8>(m, a, s, W);
-        if (D <= 192) return launch_group_t<float, 12>(m, a, s, W);
+        if (D <= 32) return launch_cc_t<float, 2>(m, a, s, W);
+        if (D <= 64) return launch_cc_t<float, 4>(m, a, s, W);
+        if (D <= 96) return launch_cc_t<float, 6>(m, a, s, W);
+        if (D <= 128) return launch_cc_t<float, 8>(m, a, s, W);
+        if (D <= 192) return launch_cc_t<float, 12>(m, a, s, W);
     }
     *why = "slip dimension too large for the shared-memory inner kernel";
     return cudaErrorInvalidValue;

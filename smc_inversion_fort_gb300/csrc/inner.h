@@ -12,7 +12,8 @@ namespace smc {
 struct InnerArgs {
     int n_theta, N, NP2, D, mixed;
     int ntau, tf, max_stages;
-    int warps_per_theta;  // warps per geometry in the inner kernel (1, 2, 4, 8; 0 picks by batch size)
+    int warps_per_theta;  // CUDA-core engine: warps per geometry (1, 2, 4, 8; 0 picks by batch size)
+    int engine;           // MIXED step engine, SMCGPU_ENGINE_* (tensor-core engines need D <= 128)
     double cv, max_slip;
     uint64_t seed;
     const unsigned long long *streams;  // [n_theta]

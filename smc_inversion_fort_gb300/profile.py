@@ -1,7 +1,7 @@
 """Fixed small workloads for profiling one kernel family at a time.
 
     python -m smc_inversion_fort_gb300.profile greens [--n-theta 256] [--fp32] [--reps 2]
-    python -m smc_inversion_fort_gb300.profile nested [--n-theta 16] [--mixed] [--reps 1] [--warps 0]
+    python -m smc_inversion_fort_gb300.profile nested [--n-theta 16] [--mixed] [--reps 1] [--warps 0] [--engine mma|cuda|tcgen05]
 
 `greens` runs the Green's build of the 16x8-patch, 5x5-Gauss-point,
 400-station workload on n geometries; `nested` runs nested evaluations of the
@@ -23,6 +23,7 @@ def main(argv=None):
     p.add_argument("--mixed", action="store_true")
     p.add_argument("--reps", type=int, default=2)
     p.add_argument("--warps", type=int, default=0, help="inner kernel warps per geometry (0: by batch size)")
+    p.add_argument("--engine", choices=["mma", "cuda", "tcgen05"], default="mma", help="MIXED inner step engine")
     a = p.parse_args(argv)
     import torch
 
@@ -49,6 +50,7 @@ def main(argv=None):
     else:
         w = preset("c0")
         w.settings.inner_warps = a.warps
+        w.settings.inner_engine = {"mma": 0, "cuda": 1, "tcgen05": 2}[a.engine]
         n = a.n_theta or 16
         rng = np.random.default_rng(2024)
         obs = make_stations(w, rng)
@@ -63,7 +65,7 @@ def main(argv=None):
         for r in range(a.reps):
             t0 = time.perf_counter()
             nl, st = g.fault_calc_likelihood(th, 1, np.arange(n, dtype=np.uint64) + 1000 * r)
-            print(f"nested n_theta={n} warps={a.warps} {'mixed' if a.mixed else 'fp64'}: {time.perf_counter() - t0:.3f} s, "
+            print(f"nested n_theta={n} warps={a.warps} {a.engine} {'mixed' if a.mixed else 'fp64'}: {time.perf_counter() - t0:.3f} s, "
                   f"-logZ[0] {nl[0]:.4f}, status {int(st.max())}")
 
 

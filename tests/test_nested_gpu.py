@@ -66,7 +66,7 @@ def test_nested_fp64_bitwise_schedule_short_trajectories(smcgpu, orc, name, ntau
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_inner_warps_do_not_change_results(smcgpu, orc, prec):
-    """The inner kernel's warps per geometry (1, 2, 4, 8) change only which
+    """The CUDA-core engine's warps per geometry (1, 2, 4, 8) change only which
     chain slot runs which child; with short trajectories every setting gives
     the same tempering schedule and -log Z (to the rounding of the group sums
     in the bisection), and the FP64 results equal the oracle's."""
@@ -76,6 +76,7 @@ def test_inner_warps_do_not_change_results(smcgpu, orc, prec):
     th = np.vstack([true_theta(w)[None], random_thetas(w, 11, seed=5)])
     streams = np.arange(300, 300 + len(th), dtype=np.uint64)
     p = smcgpu.PREC_FP64 if prec == "fp64" else smcgpu.PREC_MIXED
+    w.settings.inner_engine = smcgpu.ENGINE_CUDA   # the engine whose warps per geometry vary
     res = {}
     for W in (1, 2, 4, 8):
         w.settings.inner_warps = W
@@ -140,9 +141,11 @@ def test_nested_fp64_statistics_match_oracle(smcgpu, orc):
     assert abs(a.mean() - b.mean()) < 4 * se + 1e-6
 
 
-def test_nested_mixed_matches_fp64(smcgpu, orc):
-    """MIXED against FP64: the mean -log Z over independent streams agrees
-    within 4 standard errors (and within 1 nat)."""
+@pytest.mark.parametrize("engine", ["mma", "cuda", "tcgen05"])
+def test_nested_mixed_matches_fp64(smcgpu, orc, engine):
+    """MIXED against FP64, for every leapfrog engine (warp-level BF16x3 MMA,
+    FP32 CUDA cores, BF16x3 tcgen05): the mean -log Z over independent
+    streams agrees within 4 standard errors (and the medians within 1 nat)."""
     w, obs, o = setup_case("tiny", orc)
     th = np.vstack([true_theta(w)[None], random_thetas(w, 3, seed=4)])
     reps = 48
@@ -150,7 +153,9 @@ def test_nested_mixed_matches_fp64(smcgpu, orc):
     streams = np.arange(len(th_rep), dtype=np.uint64) + 5000
     g64 = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
     g64.set_data(obs)
-    g32 = smcgpu.SmcGpu(w.settings, smcgpu.PREC_MIXED)
+    import dataclasses
+    s32 = dataclasses.replace(w.settings, inner_engine={"mma": 0, "cuda": 1, "tcgen05": 2}[engine])
+    g32 = smcgpu.SmcGpu(s32, smcgpu.PREC_MIXED)
     g32.set_data(obs)
     a, sa = g64.fault_calc_likelihood(th_rep, 21, streams)
     b, sb = g32.fault_calc_likelihood(th_rep, 21, streams)
