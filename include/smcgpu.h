@@ -17,6 +17,7 @@
  *                              (discretize_fault, gen_laplacian, calc_greens_func,
  *                              slip_smc_exec for every theta in one call)
  *   smcgpu_fault_smc_exec      smc_fault.f90:785-1075 fault_smc_exec
+ *   smcgpu_fault_smc_exec_gsmc the same with gsmc = .true. (smc_fault.f90:9-52)
  *   smcgpu_resample_counts     smc_slip.f90:572-589 / smc_fault.f90:572-590
  *   smcgpu_qsort_              sort.cpp:3-7 qsort_ (same symbol shape)
  *   smcgpu_read_*              main.f90:107-157, init.f90:5-80 (input files)
@@ -181,11 +182,25 @@ int32_t smcgpu_fault_likelihood_posterior(smcgpu_ctx *ctx, const double *theta, 
 /* The full outer SMC (fault_smc_exec, smc_fault.f90:785-1075) with a uniform
  * prior box range(2, ndim_fault).  particles_out(ndim_fault, nparticle) and
  * likelihood_out(nparticle) receive the final population.  When output_dir
- * is not NULL, the reference's per-stage CSV files <iter>.csv are written
- * there (smc_fault.f90:923-936, 1054-1067). */
+ * is not NULL, the reference's per-stage CSV files output_dir<iter>.csv are
+ * written (the name is the prefix and the stage number concatenated, as
+ * trim(output_dir)//iter//".csv" in smc_fault.f90:923-936, 1054-1067; the
+ * directory is created like main.f90's "mkdir -p"). */
 int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, int32_t nparticle, uint64_t seed,
                               const char *output_dir, double *particles_out, double *likelihood_out,
                               double *evidence_out, int32_t *nstage_out);
+
+/* The outer SMC in GSMC mode (gsmc = .true., main.f90:313-330): the initial
+ * population is drawn from q = N(qmean, qcov) and the tempering runs from q
+ * to the posterior, i.e. on L - q (smc_fault.f90:9-52, 392-485, 748-771).
+ * qcov_chol is the lower Cholesky factor of qcov (the reference's qcov after
+ * dpotrf('L')), qcov_inv its inverse, both ndim x ndim column-major, and
+ * log_qcov_det = log det qcov, as in data/qcov.dat, qcov_inv.dat and
+ * log_qcov_det.dat.  range still bounds the random-walk proposals. */
+int32_t smcgpu_fault_smc_exec_gsmc(smcgpu_ctx *ctx, const double *range, int32_t nparticle, uint64_t seed,
+                                   const char *output_dir, const double *qmean, const double *qcov_chol,
+                                   const double *qcov_inv, double log_qcov_det, double *particles_out,
+                                   double *likelihood_out, double *evidence_out, int32_t *nstage_out);
 
 /* Residual-systematic resampling counts on the device (smc_slip.f90:572-589).
  * u0 is the binary128 uniform of random_number_correction_dd carried as a

@@ -101,7 +101,7 @@ extern "C" void orc_quad_uniform(uint64_t seed, uint64_t stream, uint32_t purpos
 enum {
     RNG_GIBBS = 1, RNG_TUNE_DTAU = 2, RNG_TUNE_MOM = 3, RNG_TUNE_MH = 4, RNG_TUNE_RES = 5,
     RNG_SMP_MOM = 6, RNG_SMP_MH = 7, RNG_RESAMPLE = 8,
-    RNG_OUT_INIT = 16, RNG_OUT_RES = 17, RNG_OUT_PROP = 18, RNG_OUT_MH = 19
+    RNG_OUT_INIT = 16, RNG_OUT_RES = 17, RNG_OUT_PROP = 18, RNG_OUT_MH = 19, RNG_OUT_QINIT = 20
 };
 static const uint64_t OUTER_STREAM = ~0ull;
 static inline uint64_t eval_stream(uint32_t iter, uint32_t kind, uint64_t slot) {
@@ -1374,38 +1374,74 @@ static int cholesky_lower(double *a, int n) {   // dpotrf('L'), column-major
     return 0;
 }
 
+// dtrmv('l','n','n'): z := L z with L lower-triangular, column-major (the
+// reference BLAS column order)
+static void trmv_lower(const double *L, int nd, double *z) {
+    for (int jj = nd - 1; jj >= 0; --jj) {
+        double t = z[jj];
+        for (int ii = nd - 1; ii > jj; --ii) z[ii] += t * L[(size_t)jj * nd + ii];
+        z[jj] *= L[(size_t)jj * nd + jj];
+    }
+}
+
+// fault_calc_neglog_q (smc_fault.f90:9-27): -log N(x; qmean, qcov)
+static double neglog_q(const orc_gsmc *q, const double *x, int nd) {
+    double pi = 2.0 * asin(1.0);
+    std::vector<double> delta(nd);
+    for (int d = 0; d < nd; ++d) delta[d] = x[d] - q->qmean[d];
+    double tmp = 0.0;
+    for (int j = 0; j < nd; ++j)
+        for (int i = 0; i < nd; ++i) tmp = tmp + delta[i] * q->qcov_inv[(size_t)j * nd + i] * delta[j];
+    return tmp / 2.0 + log(2.0 * pi) * nd / 2.0 + q->log_qcov_det / 2.0;
+}
+
 extern "C" int orc_fault_smc(const orc_setup *s, const double *range, int32_t N, int32_t numprocs,
                              uint64_t seed, int32_t nthreads, double *particles_out, double *likelihood_out,
-                             double *evidence_out, int32_t *nstage_out, double *gamma_out) {
+                             double *evidence_out, int32_t *nstage_out, double *gamma_out, const orc_gsmc *gq) {
     int nd = ndim_fault_of(s);
-    std::vector<double> parts((size_t)N * nd), Ls(N), w(N), mean(nd), cov((size_t)nd * nd);
+    std::vector<double> parts((size_t)N * nd), Ls(N), w(N), mean(nd), cov((size_t)nd * nd), qs(N, 0.0);
     std::vector<int32_t> assigned(N), sorted(N);
     int status = 0;
-    for (int i = 0; i < N; ++i)
-        for (int d = 0; d < nd; ++d) {
-            double u = orc_uniform(seed, OUTER_STREAM, RNG_OUT_INIT, 0, i, d);
-            parts[(size_t)i * nd + d] = range[2 * d] + u * (range[2 * d + 1] - range[2 * d]);
+    // fault_sample_init_particles (smc_fault.f90:29-64)
+    if (gq) {
+        std::vector<double> z(nd);
+        for (int i = 0; i < N; ++i) {
+            for (int d = 0; d < nd; ++d) z[d] = orc_normal(seed, OUTER_STREAM, RNG_OUT_QINIT, 0, i, d);
+            trmv_lower(gq->qcov_chol, nd, z.data());
+            for (int d = 0; d < nd; ++d) parts[(size_t)i * nd + d] = z[d] + gq->qmean[d];
         }
+    } else {
+        for (int i = 0; i < N; ++i)
+            for (int d = 0; d < nd; ++d) {
+                double u = orc_uniform(seed, OUTER_STREAM, RNG_OUT_INIT, 0, i, d);
+                parts[(size_t)i * nd + d] = range[2 * d] + u * (range[2 * d + 1] - range[2 * d]);
+            }
+    }
     {
         std::vector<uint64_t> st(N);
         std::vector<int32_t> stv(N);
         for (int i = 0; i < N; ++i) st[i] = eval_stream(0, 0, i);
         orc_fault_likelihood_batch(s, N, parts.data(), seed, st.data(), Ls.data(), stv.data(), nthreads);
         for (int i = 0; i < N; ++i) status |= stv[i];
+        // work_eval_init_particles (smc_fault.f90:350-353)
+        if (gq)
+            for (int i = 0; i < N; ++i) qs[i] = neglog_q(gq, &parts[(size_t)i * nd], nd);
     }
     double gamma = 0.0, evidence = 0.0;
     int iter = 1;
     while (1.0 - gamma > pow(10.0, -8.0)) {
         if (s->max_outer_stages != 0 && iter > std::max(s->max_outer_stages, 0)) break;
-        // fault_find_next_gamma (:392-485)
-        double gprev = gamma, minL = Ls[0];
-        for (int i = 0; i < N; ++i) minL = std::min(minL, Ls[i]);
+        // fault_find_next_gamma (:392-485); GSMC tempers L - q
+        std::vector<double> nlr(N);
+        for (int i = 0; i < N; ++i) nlr[i] = gq ? Ls[i] - qs[i] : Ls[i];
+        double gprev = gamma, minL = nlr[0];
+        for (int i = 0; i < N; ++i) minL = std::min(minL, nlr[i]);
         double lower = gprev, upper = 1.0, err = 1.0, dg;
         int cnt = 0;
         while (err > pow(10.0, -8.0)) {
             gamma = (lower + upper) / 2.0;
             dg = gamma - gprev;
-            for (int i = 0; i < N; ++i) w[i] = exp(-dg * (Ls[i] - minL));
+            for (int i = 0; i < N; ++i) w[i] = exp(-dg * (nlr[i] - minL));
             double m = 0.0;
             for (int i = 0; i < N; ++i) m = m + w[i];
             m = m / N;
@@ -1421,7 +1457,7 @@ extern "C" int orc_fault_smc(const orc_setup *s, const double *range, int32_t N,
         }
         double ev = 0.0;
         dg = gamma - gprev;
-        for (int i = 0; i < N; ++i) ev = ev + exp(-dg * (Ls[i] - minL));
+        for (int i = 0; i < N; ++i) ev = ev + exp(-dg * (nlr[i] - minL));
         ev = ev / N;
         evidence = evidence - log(ev) + dg * minL;
         if (gamma_out && iter <= 1024) gamma_out[iter - 1] = gamma;
@@ -1447,7 +1483,7 @@ extern "C" int orc_fault_smc(const orc_setup *s, const double *range, int32_t N,
         // fault_reorder_to_send (:592-637) with qsort_ (sort.cpp)
         {
             std::vector<int32_t> ta = assigned;
-            std::vector<double> tp = parts, tl = Ls;
+            std::vector<double> tp = parts, tl = Ls, tq = qs;
             for (int i = 0; i < N; ++i) sorted[i] = i + 1;
             int32_t nn = N;
             orc_qsort_(assigned.data(), sorted.data(), &nn);
@@ -1459,6 +1495,7 @@ extern "C" int orc_fault_smc(const orc_setup *s, const double *range, int32_t N,
                     assigned[nw] = ta[org];
                     for (int d = 0; d < nd; ++d) parts[(size_t)nw * nd + d] = tp[(size_t)org * nd + d];
                     Ls[nw] = tl[org];
+                    qs[nw] = tq[org];
                 }
         }
         // work_mcmc_sampling (:639-783): parents re-evaluated, then chained MH
@@ -1467,7 +1504,7 @@ extern "C" int orc_fault_smc(const orc_setup *s, const double *range, int32_t N,
         std::vector<int32_t> start(N);
         start[0] = 0;
         for (int i = 0; i < N - 1; ++i) start[i + 1] = start[i] + assigned[i];
-        std::vector<double> curp = parts, Lcur(N), newp((size_t)N * nd), newL(N);
+        std::vector<double> curp = parts, Lcur(N), newp((size_t)N * nd), newL(N), qcur = qs, newq(N, 0.0);
         {
             std::vector<uint64_t> st(N);
             std::vector<int32_t> stv(N);
@@ -1486,12 +1523,7 @@ extern "C" int orc_fault_smc(const orc_setup *s, const double *range, int32_t N,
                 int j = start[i] + r;
                 std::vector<double> z(nd), x(nd);
                 for (int d = 0; d < nd; ++d) z[d] = orc_normal(seed, OUTER_STREAM, RNG_OUT_PROP, iter, j, d);
-                // dtrmv('l','n','n'): z := L z (reference BLAS column order)
-                for (int jj = nd - 1; jj >= 0; --jj) {
-                    double t = z[jj];
-                    for (int ii = nd - 1; ii > jj; --ii) z[ii] += t * cov[(size_t)jj * nd + ii];
-                    z[jj] *= cov[(size_t)jj * nd + jj];
-                }
+                trmv_lower(cov.data(), nd, z.data());
                 for (int d = 0; d < nd; ++d) x[d] = curp[(size_t)i * nd + d] + z[d];
                 for (int d = 0; d < nd; ++d) {
                     double lo = range[2 * d], hi = range[2 * d + 1];
@@ -1512,16 +1544,22 @@ extern "C" int orc_fault_smc(const orc_setup *s, const double *range, int32_t N,
                 status |= stv[q];
                 int i = who[q], j = start[i] + r;
                 double mh = orc_uniform(seed, OUTER_STREAM, RNG_OUT_MH, iter, j, 0);
-                if (gamma * (Lcur[i] - Lc[q]) > log(mh)) {
+                // work_mcmc_sampling's test (smc_fault.f90:748-771)
+                double qc = gq ? neglog_q(gq, &cand[(size_t)q * nd], nd) : 0.0;
+                double lhs = gq ? gamma * (Lcur[i] - Lc[q]) + (1.0 - gamma) * (qcur[i] - qc) : gamma * (Lcur[i] - Lc[q]);
+                if (lhs > log(mh)) {
                     for (int d = 0; d < nd; ++d) curp[(size_t)i * nd + d] = cand[(size_t)q * nd + d];
                     Lcur[i] = Lc[q];
+                    qcur[i] = qc;
                 }
                 newL[j] = Lcur[i];
+                newq[j] = qcur[i];
                 for (int d = 0; d < nd; ++d) newp[(size_t)j * nd + d] = curp[(size_t)i * nd + d];
             }
         }
         parts = newp;
         Ls = newL;
+        qs = newq;
         iter = iter + 1;
         if (iter > 100000) break;
     }

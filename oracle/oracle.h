@@ -105,10 +105,19 @@ int orc_greens_batch(const orc_setup *s, int32_t n, const double *theta, double 
 void orc_resample(const double *w, int32_t n, double u_hi, double u_lo, int32_t *counts);
 void orc_qsort_(int32_t *arr, int32_t *index, int32_t *n);
 
+/* GSMC reference distribution q = N(qmean, qcov) of the outer SMC
+ * (smc_fault.f90:9-27, 41-52; main.f90:313-330) */
+typedef struct orc_gsmc {
+    const double *qmean;      /* [ndim] */
+    const double *qcov_chol;  /* [ndim][ndim] lower Cholesky factor of qcov, column-major */
+    const double *qcov_inv;   /* [ndim][ndim] column-major */
+    double log_qcov_det;
+} orc_gsmc;
+
 int orc_fault_smc(const orc_setup *s, const double *range /* [ndim][2] */, int32_t nparticle,
                   int32_t numprocs, uint64_t seed, int32_t nthreads, double *particles_out,
                   double *likelihood_out, double *evidence_out, int32_t *nstage_out,
-                  double *gamma_out /* optional, 1024 */);
+                  double *gamma_out /* optional, 1024 */, const orc_gsmc *gsmc /* NULL: uniform prior */);
 
 #ifdef __cplusplus
 }

@@ -78,7 +78,7 @@ def lib() -> C.CDLL:
         L.orc_fault_likelihood_batch.argtypes = [vp, i32, vp, u64, vp, vp, vp, i32]
         L.orc_resample.argtypes = [vp, i32, d, d, vp]
         L.orc_qsort_.argtypes = [vp, vp, vp]
-        L.orc_fault_smc.argtypes = [vp, vp, i32, i32, u64, i32, vp, vp, vp, vp, vp]
+        L.orc_fault_smc.argtypes = [vp, vp, i32, i32, u64, i32, vp, vp, vp, vp, vp, vp]
         L.orc_fault_smc.restype = i32
         _lib = L
     return _lib
@@ -203,16 +203,30 @@ class Oracle:
                                          nthreads)
         return nl, stat
 
-    def fault_smc(self, range_, nparticle, seed, numprocs=1, nthreads=0):
+    def fault_smc(self, range_, nparticle, seed, numprocs=1, nthreads=0, gsmc=None):
+        """gsmc: None (uniform prior box) or dict(qmean, qcov_chol, qcov_inv, log_qcov_det)."""
         rg = np.ascontiguousarray(range_, np.float64)
         nd = self.dims["ndim_fault"]
         parts, L = np.zeros((nparticle, nd)), np.zeros(nparticle)
         ev, ns = C.c_double(), C.c_int32()
         gam = np.zeros(1024)
+        gp = None
+        if gsmc is not None:
+            keep = [np.ascontiguousarray(gsmc[k], np.float64) for k in ("qmean", "qcov_chol", "qcov_inv")]
+            # column-major matrices: pass the transpose of a row-major (nd, nd) array
+            keep[1] = np.ascontiguousarray(keep[1].T)
+            keep[2] = np.ascontiguousarray(keep[2].T)
+            g = OrcGsmc(_p(keep[0]), _p(keep[1]), _p(keep[2]), float(gsmc["log_qcov_det"]))
+            gp = C.byref(g)
         status = lib().orc_fault_smc(C.byref(self.st), _p(rg), nparticle, numprocs, seed, nthreads, _p(parts),
-                                     _p(L), C.byref(ev), C.byref(ns), _p(gam))
+                                     _p(L), C.byref(ev), C.byref(ns), _p(gam), gp)
         return {"particles": parts, "likelihood": L, "evidence": ev.value, "nstage": ns.value,
                 "gamma": gam[: ns.value].copy(), "status": status}
+
+
+class OrcGsmc(C.Structure):
+    _fields_ = [("qmean", C.c_void_p), ("qcov_chol", C.c_void_p), ("qcov_inv", C.c_void_p),
+                ("log_qcov_det", C.c_double)]
 
 
 def dc3d0(alpha, x, y, z, depth, dip, pot1, pot2, pot3, pot4):

@@ -85,6 +85,7 @@ def load_library() -> C.CDLL:
         "smcgpu_fault_likelihood_trace": (i32, [vp, i32, vp, u64, vp, vp, vp, vp, vp, vp]),
         "smcgpu_fault_likelihood_posterior": (i32, [vp, vp, u64, u64, vp, vp, vp, vp, vp]),
         "smcgpu_fault_smc_exec": (i32, [vp, vp, i32, u64, C.c_char_p, vp, vp, vp, vp]),
+        "smcgpu_fault_smc_exec_gsmc": (i32, [vp, vp, i32, u64, C.c_char_p, vp, vp, vp, d, vp, vp, vp, vp]),
         "smcgpu_resample_counts": (i32, [vp, vp, i32, d, d, vp]),
         "smcgpu_qsort_": (None, [vp, vp, vp]),
         "smcgpu_last_error": (C.c_char_p, [vp]),
@@ -108,7 +109,7 @@ EXPORTED_SYMBOLS = [
     "smcgpu_default_config", "smcgpu_create", "smcgpu_destroy", "smcgpu_set_data", "smcgpu_set_stream",
     "smcgpu_dims", "smcgpu_greens_batch", "smcgpu_greens_batch_dev", "smcgpu_fault_likelihood_batch",
     "smcgpu_fault_likelihood_batch_dev", "smcgpu_fault_likelihood_trace", "smcgpu_fault_likelihood_posterior",
-    "smcgpu_fault_smc_exec", "smcgpu_resample_counts", "smcgpu_qsort_",
+    "smcgpu_fault_smc_exec", "smcgpu_fault_smc_exec_gsmc", "smcgpu_resample_counts", "smcgpu_qsort_",
     "smcgpu_last_error", "smcgpu_read_settings", "smcgpu_settings_to_config", "smcgpu_count_observations",
     "smcgpu_read_observations", "smcgpu_read_range", "smcgpu_read_values", "smcgpu_write_slip",
 ]
@@ -255,7 +256,10 @@ class SmcGpu:
         self._check(self.lib.smcgpu_write_slip(self.h, path.encode(), len(L), _ptr(x), _ptr(L), _ptr(P)), "write_slip")
 
     # fault_smc_exec (smc_fault.f90:785-1075)
-    def fault_smc_exec(self, range_: np.ndarray, nparticle: int, seed: int, output_dir: str | None = None):
+    def fault_smc_exec(self, range_: np.ndarray, nparticle: int, seed: int, output_dir: str | None = None,
+                       gsmc: dict | None = None):
+        """gsmc: None (uniform prior box) or dict(qmean, qcov_chol, qcov_inv, log_qcov_det) with
+        (ndim, ndim) row-indexed matrices; the GSMC mode of smc_fault.f90."""
         rg = np.ascontiguousarray(range_, dtype=np.float64)
         nd = self.dims()["ndim_fault"]
         parts = np.empty((nparticle, nd), np.float64)
@@ -263,8 +267,17 @@ class SmcGpu:
         ev = C.c_double()
         ns = C.c_int32()
         od = output_dir.encode() if output_dir else None
-        self._check(self.lib.smcgpu_fault_smc_exec(self.h, _ptr(rg), nparticle, seed, od, _ptr(parts), _ptr(lik),
-                                                   C.byref(ev), C.byref(ns)), "fault_smc_exec")
+        if gsmc is None:
+            rc = self.lib.smcgpu_fault_smc_exec(self.h, _ptr(rg), nparticle, seed, od, _ptr(parts), _ptr(lik),
+                                                C.byref(ev), C.byref(ns))
+        else:
+            qm = np.ascontiguousarray(gsmc["qmean"], np.float64)
+            qc = np.ascontiguousarray(np.asarray(gsmc["qcov_chol"], np.float64).T)   # column-major
+            qi = np.ascontiguousarray(np.asarray(gsmc["qcov_inv"], np.float64).T)
+            rc = self.lib.smcgpu_fault_smc_exec_gsmc(self.h, _ptr(rg), nparticle, seed, od, _ptr(qm), _ptr(qc),
+                                                     _ptr(qi), float(gsmc["log_qcov_det"]), _ptr(parts), _ptr(lik),
+                                                     C.byref(ev), C.byref(ns))
+        self._check(rc, "fault_smc_exec")
         return parts, lik, ev.value, ns.value
 
     # slip_resample_particles / fault_resample_particles (binary128-exact counts)

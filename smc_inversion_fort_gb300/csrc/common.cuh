@@ -21,7 +21,7 @@ namespace smc {
 enum RngPurpose : uint32_t {
     RNG_GIBBS = 1, RNG_TUNE_DTAU = 2, RNG_TUNE_MOM = 3, RNG_TUNE_MH = 4, RNG_TUNE_RES = 5,
     RNG_SMP_MOM = 6, RNG_SMP_MH = 7, RNG_RESAMPLE = 8,
-    RNG_OUT_INIT = 16, RNG_OUT_RES = 17, RNG_OUT_PROP = 18, RNG_OUT_MH = 19
+    RNG_OUT_INIT = 16, RNG_OUT_RES = 17, RNG_OUT_PROP = 18, RNG_OUT_MH = 19, RNG_OUT_QINIT = 20
 };
 static constexpr uint64_t OUTER_STREAM = ~0ull;
 

@@ -270,9 +270,35 @@ static void write_stage_csv(const char *dir, int iter, const std::vector<double>
     std::fclose(f);
 }
 
-extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, int32_t N, uint64_t seed,
-                                         const char *output_dir, double *particles_out, double *likelihood_out,
-                                         double *evidence_out, int32_t *nstage_out) {
+// GSMC reference distribution q = N(qmean, qcov) (smc_fault.f90:9-52)
+struct GsmcQ {
+    const double *qmean, *qcov_chol, *qcov_inv;
+    double log_qcov_det;
+};
+
+// dtrmv('l','n','n'): z := L z, L lower-triangular column-major (reference BLAS column order)
+static void trmv_lower(const double *L, int nd, double *z) {
+    for (int jj = nd - 1; jj >= 0; --jj) {
+        double t = z[jj];
+        for (int ii = nd - 1; ii > jj; --ii) z[ii] += t * L[(size_t)jj * nd + ii];
+        z[jj] *= L[(size_t)jj * nd + jj];
+    }
+}
+
+// fault_calc_neglog_q (smc_fault.f90:9-27), same loop order
+static double neglog_q(const GsmcQ &q, const double *x, int nd) {
+    const double pi = 2.0 * std::asin(1.0);
+    std::vector<double> delta(nd);
+    for (int d = 0; d < nd; ++d) delta[d] = x[d] - q.qmean[d];
+    double tmp = 0.0;
+    for (int j = 0; j < nd; ++j)
+        for (int i = 0; i < nd; ++i) tmp = tmp + delta[i] * q.qcov_inv[(size_t)j * nd + i] * delta[j];
+    return tmp / 2.0 + std::log(2.0 * pi) * nd / 2.0 + q.log_qcov_det / 2.0;
+}
+
+static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64_t seed, const char *output_dir,
+                         const GsmcQ *gq, double *particles_out, double *likelihood_out, double *evidence_out,
+                         int32_t *nstage_out) {
     if (!ctx) return SMCGPU_ERR_ARG;
     int r = check_ready(ctx);
     if (r) return r;
@@ -282,7 +308,7 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
     const int nd = ctx->mesh.ndim_fault;
     const uint64_t OS = smc::OUTER_STREAM;
     cudaStream_t s = ctx->stream;
-    std::vector<double> parts((size_t)N * nd), Ls(N), w(N), mean(nd), cov((size_t)nd * nd);
+    std::vector<double> parts((size_t)N * nd), Ls(N), w(N), mean(nd), cov((size_t)nd * nd), qs(N, 0.0);
     std::vector<int32_t> assigned(N), sorted(N);
     int status = 0;
     smc::DevBuf<double> d_th, d_nl;
@@ -307,17 +333,30 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
         for (int q = 0; q < nb; ++q) status |= stv[q];
         return SMCGPU_OK;
     };
-    // fault_sample_init_particles (smc_fault.f90:53-62)
-    for (int i = 0; i < N; ++i)
-        for (int d = 0; d < nd; ++d) {
-            double u = smc::rng_uniform(seed, OS, smc::RNG_OUT_INIT, 0, i, d);
-            parts[(size_t)i * nd + d] = range[2 * d] + u * (range[2 * d + 1] - range[2 * d]);
+    // fault_sample_init_particles (smc_fault.f90:29-64): the prior box, or
+    // N(qmean, qcov) in GSMC mode
+    if (gq) {
+        std::vector<double> z(nd);
+        for (int i = 0; i < N; ++i) {
+            for (int d = 0; d < nd; ++d) z[d] = host_normal(seed, OS, smc::RNG_OUT_QINIT, 0, i, d);
+            trmv_lower(gq->qcov_chol, nd, z.data());
+            for (int d = 0; d < nd; ++d) parts[(size_t)i * nd + d] = z[d] + gq->qmean[d];
         }
+    } else {
+        for (int i = 0; i < N; ++i)
+            for (int d = 0; d < nd; ++d) {
+                double u = smc::rng_uniform(seed, OS, smc::RNG_OUT_INIT, 0, i, d);
+                parts[(size_t)i * nd + d] = range[2 * d] + u * (range[2 * d + 1] - range[2 * d]);
+            }
+    }
     {
         std::vector<unsigned long long> sid(N);
         for (int i = 0; i < N; ++i) sid[i] = smc::eval_stream(0, 0, i);
         r = evaluate(parts, sid, Ls);
         if (r) return r;
+        // work_eval_init_particles (smc_fault.f90:350-353)
+        if (gq)
+            for (int i = 0; i < N; ++i) qs[i] = neglog_q(*gq, &parts[(size_t)i * nd], nd);
     }
     if (output_dir) write_stage_csv(output_dir, 0, parts, Ls, N, nd);
     double gamma = 0.0, evidence = 0.0;
@@ -327,15 +366,17 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
     CU(ctx->d_flag.ensure(1), "alloc");
     while (1.0 - gamma > std::pow(10.0, -8.0)) {
         if (ctx->cfg.max_outer_stages != 0 && iter > std::max(ctx->cfg.max_outer_stages, 0)) break;
-        // fault_find_next_gamma (smc_fault.f90:392-485)
-        double gprev = gamma, minL = Ls[0];
-        for (int i = 0; i < N; ++i) minL = std::min(minL, Ls[i]);
+        // fault_find_next_gamma (smc_fault.f90:392-485); GSMC tempers L - q
+        std::vector<double> nlr(N);
+        for (int i = 0; i < N; ++i) nlr[i] = gq ? Ls[i] - qs[i] : Ls[i];
+        double gprev = gamma, minL = nlr[0];
+        for (int i = 0; i < N; ++i) minL = std::min(minL, nlr[i]);
         double lower = gprev, upper = 1.0, err = 1.0, dg;
         int cnt = 0;
         while (err > std::pow(10.0, -8.0)) {
             gamma = (lower + upper) / 2.0;
             dg = gamma - gprev;
-            for (int i = 0; i < N; ++i) w[i] = std::exp(-dg * (Ls[i] - minL));
+            for (int i = 0; i < N; ++i) w[i] = std::exp(-dg * (nlr[i] - minL));
             double m = 0.0;
             for (int i = 0; i < N; ++i) m = m + w[i];
             m = m / N;
@@ -351,7 +392,7 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
         }
         double ev = 0.0;
         dg = gamma - gprev;
-        for (int i = 0; i < N; ++i) ev = ev + std::exp(-dg * (Ls[i] - minL));
+        for (int i = 0; i < N; ++i) ev = ev + std::exp(-dg * (nlr[i] - minL));
         ev = ev / N;
         evidence = evidence - std::log(ev) + dg * minL;
         // fault_normalize_weights, fault_calc_mean_particles, fault_calc_cov_particles
@@ -383,7 +424,7 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
         // fault_reorder_to_send with qsort_ (one rank: the sorted order itself)
         {
             std::vector<int32_t> ta = assigned;
-            std::vector<double> tp = parts, tl = Ls;
+            std::vector<double> tp = parts, tl = Ls, tq = qs;
             for (int i = 0; i < N; ++i) sorted[i] = i + 1;
             int32_t nn = N;
             smcgpu_qsort_(assigned.data(), sorted.data(), &nn);
@@ -392,6 +433,7 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
                 assigned[k] = ta[org];
                 for (int d = 0; d < nd; ++d) parts[(size_t)k * nd + d] = tp[(size_t)org * nd + d];
                 Ls[k] = tl[org];
+                qs[k] = tq[org];
             }
         }
         // work_mcmc_sampling (smc_fault.f90:639-783): parents re-evaluated,
@@ -399,7 +441,7 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
         std::vector<int32_t> start(N);
         start[0] = 0;
         for (int i = 0; i < N - 1; ++i) start[i + 1] = start[i] + assigned[i];
-        std::vector<double> curp = parts, Lcur(N), newp((size_t)N * nd), newL(N);
+        std::vector<double> curp = parts, Lcur(N), newp((size_t)N * nd), newL(N), qcur = qs, newq(N, 0.0);
         int maxa = 0;
         for (int i = 0; i < N; ++i) maxa = std::max(maxa, (int)assigned[i]);
         for (int rr = 0; rr < std::max(maxa, 1); ++rr) {
@@ -426,11 +468,7 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
                 int j = start[i] + rr;
                 std::vector<double> z(nd), x(nd);
                 for (int d = 0; d < nd; ++d) z[d] = host_normal(seed, OS, smc::RNG_OUT_PROP, iter, j, d);
-                for (int jj = nd - 1; jj >= 0; --jj) {  // dtrmv('l','n','n')
-                    double t = z[jj];
-                    for (int ii = nd - 1; ii > jj; --ii) z[ii] += t * cov[(size_t)jj * nd + ii];
-                    z[jj] *= cov[(size_t)jj * nd + jj];
-                }
+                trmv_lower(cov.data(), nd, z.data());
                 for (int d = 0; d < nd; ++d) x[d] = curp[(size_t)i * nd + d] + z[d];
                 for (int d = 0; d < nd; ++d) {
                     double lo = range[2 * d], hi = range[2 * d + 1];
@@ -451,16 +489,22 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
                 int i = who[q], j = start[i] + rr;
                 double Lq = Lall[npar + q];
                 double mh = smc::rng_uniform(seed, OS, smc::RNG_OUT_MH, iter, j, 0);
-                if (gamma * (Lcur[i] - Lq) > std::log(mh)) {
+                // work_mcmc_sampling's test (smc_fault.f90:748-771)
+                const double qc = gq ? neglog_q(*gq, &cand[(npar + q) * nd], nd) : 0.0;
+                const double lhs = gq ? gamma * (Lcur[i] - Lq) + (1.0 - gamma) * (qcur[i] - qc) : gamma * (Lcur[i] - Lq);
+                if (lhs > std::log(mh)) {
                     for (int d = 0; d < nd; ++d) curp[(size_t)i * nd + d] = cand[(npar + q) * nd + d];
                     Lcur[i] = Lq;
+                    qcur[i] = qc;
                 }
                 newL[j] = Lcur[i];
+                newq[j] = qcur[i];
                 for (int d = 0; d < nd; ++d) newp[(size_t)j * nd + d] = curp[(size_t)i * nd + d];
             }
         }
         parts = newp;
         Ls = newL;
+        qs = newq;
         if (output_dir) write_stage_csv(output_dir, iter, parts, Ls, N, nd);
         iter = iter + 1;
         if (iter > 100000) break;
@@ -471,4 +515,21 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
     if (nstage_out) *nstage_out = iter - 1;
     if (status) ctx->err = "fault_smc_exec: status bits " + std::to_string(status);
     return SMCGPU_OK;
+}
+
+extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, int32_t N, uint64_t seed,
+                                         const char *output_dir, double *particles_out, double *likelihood_out,
+                                         double *evidence_out, int32_t *nstage_out) {
+    return outer_smc(ctx, range, N, seed, output_dir, nullptr, particles_out, likelihood_out, evidence_out,
+                     nstage_out);
+}
+
+extern "C" int32_t smcgpu_fault_smc_exec_gsmc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64_t seed,
+                                              const char *output_dir, const double *qmean, const double *qcov_chol,
+                                              const double *qcov_inv, double log_qcov_det, double *particles_out,
+                                              double *likelihood_out, double *evidence_out, int32_t *nstage_out) {
+    if (!ctx) return SMCGPU_ERR_ARG;
+    if (!qmean || !qcov_chol || !qcov_inv) return ctx->fail(SMCGPU_ERR_ARG, "fault_smc_exec_gsmc: q missing");
+    GsmcQ q{qmean, qcov_chol, qcov_inv, log_qcov_det};
+    return outer_smc(ctx, range, N, seed, output_dir, &q, particles_out, likelihood_out, evidence_out, nstage_out);
 }

@@ -164,9 +164,27 @@ struct Group {
         sync();
         if (lane == 0) scr[wl] = v;
         sync();
-        double t = 0.0;
-        for (int w = 0; w < W; ++w) t += scr[w];
-        return t;
+        return wsum(lane < W ? scr[lane] : 0.0);   // warp partials combined by a second shuffle tree
+    }
+    // FP32 sums of two values in one round of barriers
+    __device__ void sum2f(float &u, float &v) const {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            u += __shfl_xor_sync(FULL, u, o);
+            v += __shfl_xor_sync(FULL, v, o);
+        }
+        if (W == 1) return;
+        float *fs = (float *)scr;
+        sync();
+        if (lane == 0) { fs[wl] = u; fs[W + wl] = v; }
+        sync();
+        u = lane < W ? fs[lane] : 0.0f;
+        v = lane < W ? fs[W + lane] : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            u += __shfl_xor_sync(FULL, u, o);
+            v += __shfl_xor_sync(FULL, v, o);
+        }
     }
     // two sums in one round of barriers
     __device__ void sum2(double &u, double &v) const {
@@ -176,10 +194,8 @@ struct Group {
         sync();
         if (lane == 0) { scr[wl] = u; scr[W + wl] = v; }
         sync();
-        double tu = 0.0, tv = 0.0;
-        for (int w = 0; w < W; ++w) { tu += scr[w]; tv += scr[W + w]; }
-        u = tu;
-        v = tv;
+        u = wsum(lane < W ? scr[lane] : 0.0);
+        v = wsum(lane < W ? scr[W + lane] : 0.0);
     }
     __device__ double min(double v) const {
         v = wmin(v);
@@ -187,9 +203,7 @@ struct Group {
         sync();
         if (lane == 0) scr[wl] = v;
         sync();
-        double t = scr[0];
-        for (int w = 1; w < W; ++w) t = fmin(t, scr[w]);
-        return t;
+        return wmin(lane < W ? scr[lane] : 1e300);
     }
     __device__ dd sum_dd(dd v) const {
         v = wsum_dd(v);
@@ -198,9 +212,7 @@ struct Group {
         sync();
         if (lane == 0) s[wl] = v;
         sync();
-        dd t = s[0];
-        for (int w = 1; w < W; ++w) t = dd_add(t, s[w]);
-        return t;
+        return wsum_dd(lane < W ? s[lane] : dd{0.0, 0.0});
     }
 };
 
@@ -451,21 +463,23 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
             g = (lower + upper) / 2.0;
             double dg = g - gprev, cv;
             if (MIXED) {
+                // weights in (0, 1] summed in FP32: the CV target (2) keeps
+                // s2/N - mean^2 well away from cancellation
                 float dgf = (float)dg;
-                double ps = 0.0, ps2 = 0.0;
+                float ps = 0.0f, ps2 = 0.0f;
 #pragma unroll
                 for (int q = 0; q < LR; ++q)
                     if (gt + q * gnt < N) {
                         float wk = expf(-dgf * lr[q]);
                         ps += wk;
-                        ps2 += (double)wk * wk;
+                        ps2 = fmaf(wk, wk, ps2);
                     }
                 for (int k = gt + LR * gnt; k < N; k += gnt) {
                     float wk = expf(-dgf * (float)(Lc[k] - lmin));
                     ps += wk;
-                    ps2 += (double)wk * wk;
+                    ps2 = fmaf(wk, wk, ps2);
                 }
-                grp.sum2(ps, ps2);
+                grp.sum2f(ps, ps2);
                 double s1 = ps, s2 = ps2;
                 double mean = s1 / N;
                 cv = sqrt(fmax(s2 / N - mean * mean, 0.0)) / mean;

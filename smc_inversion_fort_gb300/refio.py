@@ -114,13 +114,27 @@ def run_main(workdir: str, precision: int = PREC_FP64, seed: int = 1, stream: in
     return post
 
 
+def read_gsmc(workdir: str, nd: int) -> dict:
+    """GSMC reference distribution files (main.f90:313-332): data/qmean.dat,
+    qcov.dat, qcov_inv.dat (column-major lists), log_qcov_det.dat; qcov is
+    factored like dpotrf('L')."""
+    d = os.path.join(workdir, "data")
+    qmean = read_values(os.path.join(d, "qmean.dat"), nd, one_per_record=False)
+    qcov = read_values(os.path.join(d, "qcov.dat"), nd * nd, one_per_record=False).reshape(nd, nd).T
+    qinv = read_values(os.path.join(d, "qcov_inv.dat"), nd * nd, one_per_record=False).reshape(nd, nd).T
+    ld = read_values(os.path.join(d, "log_qcov_det.dat"), 1)[0]
+    return {"qmean": qmean, "qcov_chol": np.linalg.cholesky(qcov), "qcov_inv": qinv, "log_qcov_det": ld}
+
+
 def run_fault_smc(workdir: str, precision: int = PREC_FP64, seed: int = 1) -> dict:
-    """fault_smc_exec over data/range.dat with nparticle_fault outer particles;
-    stage CSVs go to output_dir (relative to the run directory)."""
+    """fault_smc_exec over data/range.dat with nparticle_fault outer particles
+    (GSMC when setting.dat says so); stage CSVs go to output_dir (relative to
+    the run directory)."""
     st, obs, g = load_run(workdir, precision)
     nd = g.dims()["ndim_fault"]
     rg = read_range(os.path.join(workdir, "data", "range.dat"), nd)
     od = os.path.join(workdir, st["output_dir"]) if st["output_dir"] else None
-    parts, lik, ev, ns = g.fault_smc_exec(rg, st["nparticle_fault"], seed, od)
+    gq = read_gsmc(workdir, nd) if st["gsmc"] else None
+    parts, lik, ev, ns = g.fault_smc_exec(rg, st["nparticle_fault"], seed, od, gsmc=gq)
     g.close()
     return {"particles": parts, "likelihood": lik, "evidence": ev, "nstage": ns, "range": rg}
