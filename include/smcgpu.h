@@ -21,6 +21,8 @@
  *   smcgpu_resample_counts     smc_slip.f90:572-589 / smc_fault.f90:572-590
  *   smcgpu_qsort_              sort.cpp:3-7 qsort_ (same symbol shape)
  *   smcgpu_read_*              main.f90:107-157, init.f90:5-80 (input files)
+ *   smcgpu_slip_map, smcgpu_point_cloud
+ *                              main.f90:553-830 calc_slip_map, point_cloud
  */
 #ifndef SMCGPU_H
 #define SMCGPU_H
@@ -262,6 +264,29 @@ int32_t smcgpu_read_values(const char *path, int32_t n, int32_t one_per_record, 
  * nparticle (column-major), e.g. from smcgpu_fault_likelihood_posterior. */
 int32_t smcgpu_write_slip(smcgpu_ctx *ctx, const char *path, int32_t nparticle, const double *particles,
                           const double *likelihood, const double *prior);
+
+/* ---- post-processing of sampled geometries (main.f90:553-830) */
+
+/* calc_slip_map (main.f90:553-664) on the device: one nested evaluation per
+ * theta (as fault_likelihood_batch) and the mean of its final inner
+ * population, mean_slip_out(D, n_theta) in the DOF layout. */
+int32_t smcgpu_slip_map(smcgpu_ctx *ctx, int32_t n_theta, const double *theta, uint64_t seed, const uint64_t *streams,
+                        double *mean_slip_out, double *neglog_out, int32_t *status_out);
+/* DOF vectors (D, n) to slip_dist(2, nnode, n): zero on nodes without a DOF
+ * (the patch basis is copied unchanged, D values per theta). */
+int32_t smcgpu_slip_to_nodes(const smcgpu_ctx *ctx, int32_t n, const double *slip, double *slip_nodes);
+/* calc_slip_map's output file: per theta the node slips (2 x nnode), f12.5. */
+int32_t smcgpu_write_slip_map(smcgpu_ctx *ctx, const char *path, int32_t n, const double *mean_slip);
+/* point_cloud (main.f90:666-806) on the device: every patch of every theta
+ * split into nr x nr sub-points at the cell centres of [-1, 1]^2, each with
+ * its global (x, y, z) and bilinearly interpolated slip (uxi, ueta, |u|).
+ * slip is slip_dist(2, nnode, n_theta) (the patch basis: (D, n_theta));
+ * points_out(6, nr, nr, npatch, n_theta).  The plane record (centre, strike,
+ * dip, size) is calc_greens_func's (gfunc.f90:283-296). */
+int32_t smcgpu_point_cloud(smcgpu_ctx *ctx, int32_t n_theta, const double *theta, const double *slip, int32_t nr,
+                           double *points_out);
+/* point_cloud's files: prefix//iplane (I1) per plane, records of 6 x f12.5. */
+int32_t smcgpu_write_point_cloud(smcgpu_ctx *ctx, const char *prefix, int32_t n, int32_t nr, const double *points);
 
 /* Last error message of the context (or, when ctx is NULL, of the last
  * create call or file reader on this thread). */

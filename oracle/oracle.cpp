@@ -593,6 +593,57 @@ extern "C" int orc_dims(const orc_setup *s, orc_dims_t *out) {
     return 0;
 }
 
+// point_cloud (main.f90:666-781).  The reference reads each plane's centre,
+// strike, dip and size from an 8-entries-per-plane theta that none of its
+// get_geometry layouts produces; the plane record of calc_greens_func
+// (gfunc.f90:283-296) is the one that describes the sampled fault.
+extern "C" int orc_point_cloud(const orc_setup *s, const double *theta, const double *slip, int32_t nr,
+                               double *points) {
+    std::vector<Plane> pl;
+    planes_of(s, theta, pl);
+    Mesh m;
+    discretize(s, pl, m);
+    double pi = 4.0 * atan(1.0);
+    std::vector<double> rv(nr);
+    for (int ir = 1; ir <= nr; ++ir) rv[ir - 1] = -1.0 + 1.0 / (double)nr + (ir - 1) * 2.0 / (double)nr;
+    int off_patch = 0;
+    for (int ip = 0; ip < s->nplane; ++ip) {
+        double strike_rad = pl[ip].strike * pi / 180.0, dip_rad = pl[ip].dip * pi / 180.0;
+        for (int ie = off_patch; ie < off_patch + pl[ip].nxi * pl[ip].neta; ++ie) {
+            double xin[4], etan[4], uxn[4], uen[4];
+            for (int k = 0; k < 4; ++k) {
+                int node = m.cny[4 * ie + k];
+                xin[k] = m.coor[2 * node];
+                etan[k] = m.coor[2 * node + 1];
+                uxn[k] = s->basis == 0 ? slip[2 * node] : slip[2 * ie];
+                uen[k] = s->basis == 0 ? slip[2 * node + 1] : slip[2 * ie + 1];
+            }
+            for (int ir1 = 0; ir1 < nr; ++ir1)
+                for (int ir2 = 0; ir2 < nr; ++ir2) {
+                    double r1 = rv[ir1], r2 = rv[ir2];
+                    double nv[4] = {(1.0 - r1) * (1.0 - r2) / 4.0, (1.0 + r1) * (1.0 - r2) / 4.0,
+                                    (1.0 + r1) * (1.0 + r2) / 4.0, (1.0 - r1) * (1.0 + r2) / 4.0};
+                    double xi = 0.0, eta = 0.0, uxi = 0.0, ueta = 0.0;
+                    for (int k = 0; k < 4; ++k) {
+                        xi = xi + nv[k] * xin[k];
+                        eta = eta + nv[k] * etan[k];
+                        uxi = uxi + nv[k] * uxn[k];
+                        ueta = ueta + nv[k] * uen[k];
+                    }
+                    double *o = points + (((size_t)ie * nr + ir1) * nr + ir2) * 6;
+                    o[0] = pl[ip].xf - eta * cos(dip_rad) * cos(strike_rad) + xi * sin(strike_rad);
+                    o[1] = pl[ip].yf + eta * cos(dip_rad) * sin(strike_rad) + xi * cos(strike_rad);
+                    o[2] = pl[ip].zf + eta * sin(dip_rad);
+                    o[3] = uxi;
+                    o[4] = ueta;
+                    o[5] = sqrt(uxi * uxi + ueta * ueta);
+                }
+        }
+        off_patch += pl[ip].nxi * pl[ip].neta;
+    }
+    return 0;
+}
+
 extern "C" void orc_plane_params(const orc_setup *s, const double *theta, double *out) {
     std::vector<Plane> pl;
     planes_of(s, theta, pl);

@@ -105,6 +105,11 @@ int orc_greens_batch(const orc_setup *s, int32_t n, const double *theta, double 
 void orc_resample(const double *w, int32_t n, double u_hi, double u_lo, int32_t *counts);
 void orc_qsort_(int32_t *arr, int32_t *index, int32_t *n);
 
+/* point_cloud (main.f90:666-781): sub-points of every patch with global
+ * coordinates and interpolated slip; slip is slip_dist(2, nnode) (nodal) or
+ * the D patch values; points [npatch][nr][nr][6] = x, y, z, uxi, ueta, |u| */
+int orc_point_cloud(const orc_setup *s, const double *theta, const double *slip, int32_t nr, double *points);
+
 /* GSMC reference distribution q = N(qmean, qcov) of the outer SMC
  * (smc_fault.f90:9-27, 41-52; main.f90:313-330) */
 typedef struct orc_gsmc {

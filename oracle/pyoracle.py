@@ -80,6 +80,8 @@ def lib() -> C.CDLL:
         L.orc_qsort_.argtypes = [vp, vp, vp]
         L.orc_fault_smc.argtypes = [vp, vp, i32, i32, u64, i32, vp, vp, vp, vp, vp, vp]
         L.orc_fault_smc.restype = i32
+        L.orc_point_cloud.argtypes = [vp, vp, vp, i32, vp]
+        L.orc_point_cloud.restype = i32
         _lib = L
     return _lib
 
@@ -202,6 +204,14 @@ class Oracle:
         lib().orc_fault_likelihood_batch(C.byref(self.st), th.shape[0], _p(th), seed, _p(st), _p(nl), _p(stat),
                                          nthreads)
         return nl, stat
+
+    def point_cloud(self, theta, slip, nr):
+        """slip: slip_dist(2, nnode) as a flat array (nodal) or the D patch values."""
+        th = np.ascontiguousarray(theta, np.float64)
+        sl = np.ascontiguousarray(slip, np.float64)
+        out = np.zeros((self.dims["npatch"], nr, nr, 6))
+        lib().orc_point_cloud(C.byref(self.st), _p(th), _p(sl), nr, _p(out))
+        return out
 
     def fault_smc(self, range_, nparticle, seed, numprocs=1, nthreads=0, gsmc=None):
         """gsmc: None (uniform prior box) or dict(qmean, qcov_chol, qcov_inv, log_qcov_det)."""

@@ -96,6 +96,11 @@ def load_library() -> C.CDLL:
         "smcgpu_read_range": (i32, [C.c_char_p, i32, vp]),
         "smcgpu_read_values": (i32, [C.c_char_p, i32, i32, vp]),
         "smcgpu_write_slip": (i32, [vp, C.c_char_p, i32, vp, vp, vp]),
+        "smcgpu_slip_map": (i32, [vp, i32, vp, u64, vp, vp, vp, vp]),
+        "smcgpu_slip_to_nodes": (i32, [vp, i32, vp, vp]),
+        "smcgpu_write_slip_map": (i32, [vp, C.c_char_p, i32, vp]),
+        "smcgpu_point_cloud": (i32, [vp, i32, vp, vp, i32, vp]),
+        "smcgpu_write_point_cloud": (i32, [vp, C.c_char_p, i32, i32, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -112,6 +117,8 @@ EXPORTED_SYMBOLS = [
     "smcgpu_fault_smc_exec", "smcgpu_fault_smc_exec_gsmc", "smcgpu_resample_counts", "smcgpu_qsort_",
     "smcgpu_last_error", "smcgpu_read_settings", "smcgpu_settings_to_config", "smcgpu_count_observations",
     "smcgpu_read_observations", "smcgpu_read_range", "smcgpu_read_values", "smcgpu_write_slip",
+    "smcgpu_slip_map", "smcgpu_slip_to_nodes", "smcgpu_write_slip_map", "smcgpu_point_cloud",
+    "smcgpu_write_point_cloud",
 ]
 
 
@@ -254,6 +261,48 @@ class SmcGpu:
         L = np.ascontiguousarray(likelihood, dtype=np.float64)
         P = np.ascontiguousarray(prior, dtype=np.float64)
         self._check(self.lib.smcgpu_write_slip(self.h, path.encode(), len(L), _ptr(x), _ptr(L), _ptr(P)), "write_slip")
+
+    # post-processing (main.f90:553-830)
+    def slip_map(self, theta: np.ndarray, seed: int, streams: np.ndarray):
+        """calc_slip_map: mean final inner slip population per theta -> (mean (n, D), neglog, status)."""
+        th = np.ascontiguousarray(np.atleast_2d(theta), dtype=np.float64)
+        n, D = th.shape[0], self.dims()["D"]
+        st = np.ascontiguousarray(streams, dtype=np.uint64)
+        mean, nl, stat = np.empty((n, D)), np.empty(n), np.empty(n, np.int32)
+        self._check(self.lib.smcgpu_slip_map(self.h, n, _ptr(th), seed, _ptr(st), _ptr(mean), _ptr(nl), _ptr(stat)),
+                    "slip_map")
+        return mean, nl, stat
+
+    def slip_to_nodes(self, slip: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(np.atleast_2d(slip), dtype=np.float64)
+        nn = 2 * self.mesh_counts()["nnode"] if self.settings.basis == 0 else x.shape[1]
+        out = np.empty((x.shape[0], nn))
+        self._check(self.lib.smcgpu_slip_to_nodes(self.h, x.shape[0], _ptr(x), _ptr(out)), "slip_to_nodes")
+        return out
+
+    def write_slip_map(self, path: str, mean_slip: np.ndarray):
+        x = np.ascontiguousarray(np.atleast_2d(mean_slip), dtype=np.float64)
+        self._check(self.lib.smcgpu_write_slip_map(self.h, path.encode(), x.shape[0], _ptr(x)), "write_slip_map")
+
+    def point_cloud(self, theta: np.ndarray, slip_nodes: np.ndarray, nr: int = 8) -> np.ndarray:
+        """point_cloud: (n, npatch, nr, nr, 6) = x, y, z, uxi, ueta, |u| per sub-point."""
+        th = np.ascontiguousarray(np.atleast_2d(theta), dtype=np.float64)
+        sl = np.ascontiguousarray(np.atleast_2d(slip_nodes), dtype=np.float64)
+        npatch = self.mesh_counts()["npatch"]
+        out = np.empty((th.shape[0], npatch, nr, nr, 6))
+        self._check(self.lib.smcgpu_point_cloud(self.h, th.shape[0], _ptr(th), _ptr(sl), nr, _ptr(out)), "point_cloud")
+        return out
+
+    def write_point_cloud(self, prefix: str, points: np.ndarray):
+        p = np.ascontiguousarray(points, dtype=np.float64)
+        self._check(self.lib.smcgpu_write_point_cloud(self.h, prefix.encode(), p.shape[0], p.shape[2], _ptr(p)),
+                    "write_point_cloud")
+
+    def mesh_counts(self) -> dict:
+        s = self.settings
+        nn = sum((s.nxi[i] + 1) * (s.neta[i] + 1) for i in range(s.nplane))
+        npch = sum(s.nxi[i] * s.neta[i] for i in range(s.nplane))
+        return {"nnode": nn, "npatch": npch}
 
     # fault_smc_exec (smc_fault.f90:785-1075)
     def fault_smc_exec(self, range_: np.ndarray, nparticle: int, seed: int, output_dir: str | None = None,

@@ -26,6 +26,7 @@ struct NestedOpts {
     int *nstage = nullptr;                                // device [n]
     double *particles_out = nullptr;                      // host [N][D] of theta 0 (single-theta call)
     double *lik_out = nullptr, *prior_out = nullptr;      // host [N]
+    double *mean_dev = nullptr;                           // device [n][D]: mean final inner population
 };
 
 int next_pow2(int n) {
@@ -104,6 +105,8 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
             if (why) return ctx->fail(SMCGPU_ERR_ARG, why);
             return ctx->cuda_fail(e, "inner kernel");
         }
+        if (opt.mean_dev)
+            CU(smc::launch_mean_particles(nb, N, D, ctx->d_parts.p, opt.mean_dev + (size_t)t0 * D, s), "mean kernel");
         if (opt.particles_out && t0 == 0) {
             CU(cudaMemcpyAsync(opt.particles_out, ctx->d_parts.p, (size_t)N * D * sizeof(double),
                                cudaMemcpyDeviceToHost, s), "copy particles");
@@ -532,4 +535,61 @@ extern "C" int32_t smcgpu_fault_smc_exec_gsmc(smcgpu_ctx *ctx, const double *ran
     if (!qmean || !qcov_chol || !qcov_inv) return ctx->fail(SMCGPU_ERR_ARG, "fault_smc_exec_gsmc: q missing");
     GsmcQ q{qmean, qcov_chol, qcov_inv, log_qcov_det};
     return outer_smc(ctx, range, N, seed, output_dir, &q, particles_out, likelihood_out, evidence_out, nstage_out);
+}
+
+extern "C" int32_t smcgpu_slip_map(smcgpu_ctx *ctx, int32_t n_theta, const double *theta, uint64_t seed,
+                                   const uint64_t *streams, double *mean_slip_out, double *neglog_out,
+                                   int32_t *status_out) {
+    if (!ctx) return SMCGPU_ERR_ARG;
+    int r = check_ready(ctx);
+    if (r) return r;
+    if (n_theta < 0 || (n_theta > 0 && (!theta || !streams || !mean_slip_out || !neglog_out || !status_out)))
+        return ctx->fail(SMCGPU_ERR_ARG, "slip_map: bad arguments");
+    if (n_theta == 0) return SMCGPU_OK;
+    CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+    const int nd = ctx->mesh.ndim_fault, D = ctx->mesh.D;
+    cudaStream_t s = ctx->stream;
+    smc::DevBuf<double> d_th, d_nl, d_mean;
+    smc::DevBuf<int> d_st;
+    smc::DevBuf<unsigned long long> d_sid;
+    CU(d_th.upload(theta, (size_t)n_theta * nd, s), "upload theta");
+    CU(d_sid.upload((const unsigned long long *)streams, n_theta, s), "upload streams");
+    CU(d_nl.ensure(n_theta), "alloc");
+    CU(d_st.ensure(n_theta), "alloc");
+    CU(d_mean.ensure((size_t)n_theta * D), "alloc");
+    NestedOpts opt;
+    opt.mean_dev = d_mean.p;
+    r = nested_batch(ctx, n_theta, d_th.p, seed, d_sid.p, d_nl.p, d_st.p, opt);
+    if (r) return r;
+    CU(cudaMemcpyAsync(mean_slip_out, d_mean.p, (size_t)n_theta * D * sizeof(double), cudaMemcpyDeviceToHost, s),
+       "copy");
+    CU(cudaMemcpyAsync(neglog_out, d_nl.p, (size_t)n_theta * sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
+    CU(cudaMemcpyAsync(status_out, d_st.p, (size_t)n_theta * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+    CU(cudaStreamSynchronize(s), "sync");
+    return SMCGPU_OK;
+}
+
+extern "C" int32_t smcgpu_point_cloud(smcgpu_ctx *ctx, int32_t n_theta, const double *theta, const double *slip,
+                                      int32_t nr, double *points_out) {
+    if (!ctx) return SMCGPU_ERR_ARG;
+    if (n_theta < 0 || nr < 1 || (n_theta > 0 && (!theta || !slip || !points_out)))
+        return ctx->fail(SMCGPU_ERR_ARG, "point_cloud: bad arguments");
+    if (n_theta == 0) return SMCGPU_OK;
+    CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+    const smc::MeshPattern &pm = ctx->mesh;
+    const int nd = pm.ndim_fault;
+    const int stride = ctx->cfg.basis == SMCGPU_BASIS_NODAL ? 2 * pm.nnode : pm.D;
+    cudaStream_t s = ctx->stream;
+    smc::DevBuf<double> d_th, d_slip, d_pts;
+    smc::DevBuf<smc::PlaneGeom> d_pl;
+    const size_t npts = (size_t)n_theta * pm.npatch * nr * nr;
+    CU(d_th.upload(theta, (size_t)n_theta * nd, s), "upload theta");
+    CU(d_slip.upload(slip, (size_t)n_theta * stride, s), "upload slip");
+    CU(d_pl.ensure((size_t)n_theta * pm.nplane), "alloc");
+    CU(d_pts.ensure(npts * 6), "alloc points");
+    CU(smc::launch_planes(ctx->md, n_theta, d_th.p, d_pl.p, s), "planes kernel");
+    CU(smc::launch_point_cloud(ctx->md, n_theta, d_pl.p, d_slip.p, stride, nr, d_pts.p, s), "point cloud kernel");
+    CU(cudaMemcpyAsync(points_out, d_pts.p, npts * 6 * sizeof(double), cudaMemcpyDeviceToHost, s), "copy points");
+    CU(cudaStreamSynchronize(s), "sync");
+    return SMCGPU_OK;
 }

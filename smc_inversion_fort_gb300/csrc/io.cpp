@@ -398,3 +398,76 @@ extern "C" int32_t smcgpu_write_slip(smcgpu_ctx *ctx, const char *path, int32_t 
     std::fclose(f);
     return SMCGPU_OK;
 }
+
+extern "C" int32_t smcgpu_slip_to_nodes(const smcgpu_ctx *ctx, int32_t n, const double *slip, double *slip_nodes) {
+    if (!ctx || n < 0 || (n > 0 && (!slip || !slip_nodes))) return SMCGPU_ERR_ARG;
+    // slip_dist(2, nnode) of a DOF vector (smc_slip.f90:1645-1649): zero on
+    // nodes without a DOF; the patch basis keeps its patch values
+    const smc::MeshPattern &m = ctx->mesh;
+    const bool nodal = ctx->cfg.basis == SMCGPU_BASIS_NODAL;
+    const int out_n = nodal ? 2 * m.nnode : m.D;
+    for (int t = 0; t < n; ++t) {
+        const double *x = slip + (size_t)t * m.D;
+        double *o = slip_nodes + (size_t)t * out_n;
+        if (!nodal) {
+            for (int k = 0; k < m.D; ++k) o[k] = x[k];
+            continue;
+        }
+        for (int k = 0; k < out_n; ++k) o[k] = 0.0;
+        for (int idof = 0; idof < (int)m.id_dof.size(); ++idof) {
+            o[2 * (size_t)m.id_dof[idof]] = x[2 * idof];
+            o[2 * (size_t)m.id_dof[idof] + 1] = x[2 * idof + 1];
+        }
+    }
+    return SMCGPU_OK;
+}
+
+extern "C" int32_t smcgpu_write_slip_map(smcgpu_ctx *ctx, const char *path, int32_t n, const double *mean_slip) {
+    if (!ctx) return SMCGPU_ERR_ARG;
+    if (!path || n < 0 || (n > 0 && !mean_slip)) return ctx->fail(SMCGPU_ERR_ARG, "write_slip_map: bad arguments");
+    // calc_slip_map's file (main.f90:640-664): per geometry the two slip
+    // components of every node, f12.5, then an end of record
+    const smc::MeshPattern &m = ctx->mesh;
+    const int out_n = ctx->cfg.basis == SMCGPU_BASIS_NODAL ? 2 * m.nnode : m.D;
+    std::vector<double> nodes((size_t)out_n);
+    FILE *f = std::fopen(path, "w");
+    if (!f) return ctx->fail(SMCGPU_ERR_ARG, std::string("write_slip_map: cannot open ") + path);
+    std::string line;
+    for (int t = 0; t < n; ++t) {
+        smcgpu_slip_to_nodes(ctx, 1, mean_slip + (size_t)t * m.D, nodes.data());
+        line.clear();
+        for (double v : nodes) line += smc::fortran_f(v, 12, 5);
+        line += '\n';
+        std::fputs(line.c_str(), f);
+    }
+    std::fclose(f);
+    return SMCGPU_OK;
+}
+
+extern "C" int32_t smcgpu_write_point_cloud(smcgpu_ctx *ctx, const char *prefix, int32_t n, int32_t nr,
+                                           const double *points) {
+    if (!ctx) return SMCGPU_ERR_ARG;
+    if (!prefix || n < 0 || nr < 1 || (n > 0 && !points))
+        return ctx->fail(SMCGPU_ERR_ARG, "write_point_cloud: bad arguments");
+    // point_cloud's files (main.f90:785-805): one file per plane, named
+    // prefix//iplane with iplane written as I1; records of x, y, z, uxi,
+    // ueta, |u| in f12.5, geometry by geometry, patch by patch
+    const smc::MeshPattern &m = ctx->mesh;
+    const size_t per = (size_t)m.npatch * nr * nr;
+    std::string line;
+    for (int ip = 0; ip < m.nplane; ++ip) {
+        std::string name = std::string(prefix) + (ip + 1 < 10 ? std::string(1, (char)('1' + ip)) : std::string("*"));
+        FILE *f = std::fopen(name.c_str(), "w");
+        if (!f) return ctx->fail(SMCGPU_ERR_ARG, "write_point_cloud: cannot open " + name);
+        for (int t = 0; t < n; ++t)
+            for (size_t q = (size_t)m.patch_off[ip] * nr * nr; q < (size_t)m.patch_off[ip + 1] * nr * nr; ++q) {
+                const double *pt = points + ((size_t)t * per + q) * 6;
+                line.clear();
+                for (int k = 0; k < 6; ++k) line += smc::fortran_f(pt[k], 12, 5);
+                line += '\n';
+                std::fputs(line.c_str(), f);
+            }
+        std::fclose(f);
+    }
+    return SMCGPU_OK;
+}

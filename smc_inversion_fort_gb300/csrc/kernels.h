@@ -33,4 +33,9 @@ cudaError_t launch_gram(const MeshDev &m, int n_theta, const double *gmat, const
 cudaError_t launch_resample_counts(const double *w, int n, double u_hi, double u_lo, int *counts, int *flag,
                                    cudaStream_t s);
 
+// postproc.cu: mean inner population per geometry; sub-patch slip point cloud
+cudaError_t launch_mean_particles(int n, int N, int D, const double *parts, double *out, cudaStream_t s);
+cudaError_t launch_point_cloud(const MeshDev &m, int n, const PlaneGeom *planes, const double *slip, int slip_stride,
+                               int nr, double *points, cudaStream_t s);
+
 }  // namespace smc

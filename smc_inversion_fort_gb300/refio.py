@@ -138,3 +138,49 @@ def run_fault_smc(workdir: str, precision: int = PREC_FP64, seed: int = 1) -> di
     parts, lik, ev, ns = g.fault_smc_exec(rg, st["nparticle_fault"], seed, od, gsmc=gq)
     g.close()
     return {"particles": parts, "likelihood": lik, "evidence": ev, "nstage": ns, "range": rg}
+
+
+def read_stage_samples(path: str, nparticle: int, offset: int, stride: int, nd: int) -> np.ndarray:
+    """The geometry samples that calc_slip_map / point_cloud read from an
+    outer-stage file (main.f90:575-587, 705-716): skip `offset` records,
+    then keep the last of every `stride` records; columns 1..nd of each."""
+    rows = np.loadtxt(path, ndmin=2)
+    need = offset + nparticle * stride
+    if rows.shape[0] < need:
+        raise SmcError(f"{path}: {rows.shape[0]} records, {need} needed")
+    idx = offset + stride * np.arange(1, nparticle + 1) - 1
+    return np.ascontiguousarray(rows[idx, :nd])
+
+
+def run_slip_map(workdir: str, fault_path: str, out_path: str, nparticle: int | None = None, offset: int = 10,
+                 stride: int = 2, precision: int = PREC_FP64, seed: int = 1) -> dict:
+    """calc_slip_map (main.f90:553-664) from a run directory: the mean inner
+    slip of each sampled geometry, written to out_path."""
+    st, obs, g = load_run(workdir, precision)
+    nd = g.dims()["ndim_fault"]
+    n = nparticle or st["nparticle_fault"]
+    th = read_stage_samples(os.path.join(workdir, fault_path), n, offset, stride, nd)
+    mean, nl, stat = g.slip_map(th, seed, np.arange(n, dtype=np.uint64))
+    out = os.path.join(workdir, out_path)
+    os.makedirs(os.path.dirname(out) or ".", exist_ok=True)
+    g.write_slip_map(out, mean)
+    g.close()
+    return {"theta": th, "mean_slip": mean, "neglog": nl, "status": stat}
+
+
+def run_point_cloud(workdir: str, fault_path: str, slip_path: str, out_prefix: str, nparticle: int | None = None,
+                    offset: int = 10, stride: int = 100, nr: int = 8) -> np.ndarray:
+    """point_cloud (main.f90:666-806): geometry samples from an outer-stage
+    file and their node slips from a calc_slip_map file; one output file per
+    plane, out_prefix//iplane."""
+    st, obs, g = load_run(workdir)
+    nd = g.dims()["ndim_fault"]
+    n = nparticle or st["nparticle_fault"]
+    th = read_stage_samples(os.path.join(workdir, fault_path), n, offset, stride, nd)
+    slip = np.loadtxt(os.path.join(workdir, slip_path), ndmin=2)[:n]
+    pts = g.point_cloud(th, slip, nr)
+    out = os.path.join(workdir, out_prefix)
+    os.makedirs(os.path.dirname(out) or ".", exist_ok=True)
+    g.write_point_cloud(out, pts)
+    g.close()
+    return pts
