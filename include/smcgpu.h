@@ -204,6 +204,18 @@ int32_t smcgpu_fault_smc_exec_gsmc(smcgpu_ctx *ctx, const double *range, int32_t
                                    const double *qcov_inv, double log_qcov_det, double *particles_out,
                                    double *likelihood_out, double *evidence_out, int32_t *nstage_out);
 
+/* Continue an outer SMC from the state file output_dir<k>.state that
+ * fault_smc_exec(_gsmc) writes after stage k (full-precision population,
+ * likelihoods, q values, gamma, evidence).  Draws are keyed by stage, so the
+ * continued run equals the uninterrupted one.  The GSMC parameters are given
+ * (non-NULL) exactly when the state comes from a GSMC run; nstage_out counts
+ * all stages, from the original start. */
+int32_t smcgpu_fault_smc_resume(smcgpu_ctx *ctx, const double *range, int32_t nparticle, uint64_t seed,
+                                const char *output_dir, const char *state_path, const double *qmean,
+                                const double *qcov_chol, const double *qcov_inv, double log_qcov_det,
+                                double *particles_out, double *likelihood_out, double *evidence_out,
+                                int32_t *nstage_out);
+
 /* Residual-systematic resampling counts on the device (smc_slip.f90:572-589).
  * u0 is the binary128 uniform of random_number_correction_dd carried as a
  * double-double (u0_hi + u0_lo exactly).  counts match the reference's

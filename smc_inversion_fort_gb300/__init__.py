@@ -86,6 +86,7 @@ def load_library() -> C.CDLL:
         "smcgpu_fault_likelihood_posterior": (i32, [vp, vp, u64, u64, vp, vp, vp, vp, vp]),
         "smcgpu_fault_smc_exec": (i32, [vp, vp, i32, u64, C.c_char_p, vp, vp, vp, vp]),
         "smcgpu_fault_smc_exec_gsmc": (i32, [vp, vp, i32, u64, C.c_char_p, vp, vp, vp, d, vp, vp, vp, vp]),
+        "smcgpu_fault_smc_resume": (i32, [vp, vp, i32, u64, C.c_char_p, C.c_char_p, vp, vp, vp, d, vp, vp, vp, vp]),
         "smcgpu_resample_counts": (i32, [vp, vp, i32, d, d, vp]),
         "smcgpu_qsort_": (None, [vp, vp, vp]),
         "smcgpu_last_error": (C.c_char_p, [vp]),
@@ -114,7 +115,8 @@ EXPORTED_SYMBOLS = [
     "smcgpu_default_config", "smcgpu_create", "smcgpu_destroy", "smcgpu_set_data", "smcgpu_set_stream",
     "smcgpu_dims", "smcgpu_greens_batch", "smcgpu_greens_batch_dev", "smcgpu_fault_likelihood_batch",
     "smcgpu_fault_likelihood_batch_dev", "smcgpu_fault_likelihood_trace", "smcgpu_fault_likelihood_posterior",
-    "smcgpu_fault_smc_exec", "smcgpu_fault_smc_exec_gsmc", "smcgpu_resample_counts", "smcgpu_qsort_",
+    "smcgpu_fault_smc_exec", "smcgpu_fault_smc_exec_gsmc", "smcgpu_fault_smc_resume", "smcgpu_resample_counts",
+    "smcgpu_qsort_",
     "smcgpu_last_error", "smcgpu_read_settings", "smcgpu_settings_to_config", "smcgpu_count_observations",
     "smcgpu_read_observations", "smcgpu_read_range", "smcgpu_read_values", "smcgpu_write_slip",
     "smcgpu_slip_map", "smcgpu_slip_to_nodes", "smcgpu_write_slip_map", "smcgpu_point_cloud",
@@ -261,6 +263,29 @@ class SmcGpu:
         L = np.ascontiguousarray(likelihood, dtype=np.float64)
         P = np.ascontiguousarray(prior, dtype=np.float64)
         self._check(self.lib.smcgpu_write_slip(self.h, path.encode(), len(L), _ptr(x), _ptr(L), _ptr(P)), "write_slip")
+
+    def fault_smc_resume(self, range_: np.ndarray, nparticle: int, seed: int, state_path: str,
+                         output_dir: str | None = None, gsmc: dict | None = None):
+        """Continue fault_smc_exec from a <k>.state file written after stage k."""
+        rg = np.ascontiguousarray(range_, dtype=np.float64)
+        nd = self.dims()["ndim_fault"]
+        parts = np.empty((nparticle, nd), np.float64)
+        lik = np.empty(nparticle, np.float64)
+        ev, ns = C.c_double(), C.c_int32()
+        od = output_dir.encode() if output_dir else None
+        if gsmc is None:
+            qm = qc = qi = None
+            ld = 0.0
+        else:
+            qm = np.ascontiguousarray(gsmc["qmean"], np.float64)
+            qc = np.ascontiguousarray(np.asarray(gsmc["qcov_chol"], np.float64).T)
+            qi = np.ascontiguousarray(np.asarray(gsmc["qcov_inv"], np.float64).T)
+            ld = float(gsmc["log_qcov_det"])
+        ptr = (lambda a: None if a is None else _ptr(a))
+        self._check(self.lib.smcgpu_fault_smc_resume(self.h, _ptr(rg), nparticle, seed, od, state_path.encode(),
+                                                     ptr(qm), ptr(qc), ptr(qi), ld, _ptr(parts), _ptr(lik),
+                                                     C.byref(ev), C.byref(ns)), "fault_smc_resume")
+        return parts, lik, ev.value, ns.value
 
     # post-processing (main.f90:553-830)
     def slip_map(self, theta: np.ndarray, seed: int, streams: np.ndarray):

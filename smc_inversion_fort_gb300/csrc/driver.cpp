@@ -299,9 +299,61 @@ static double neglog_q(const GsmcQ &q, const double *x, int nd) {
     return tmp / 2.0 + std::log(2.0 * pi) * nd / 2.0 + q.log_qcov_det / 2.0;
 }
 
+// Outer-SMC state after a completed stage: everything the next stage reads.
+// Written as output_dir<iter>.state next to the stage CSV (full precision,
+// where the CSV carries f20.5), so that a run can continue from any stage.
+struct OuterState {
+    int32_t nd = 0, N = 0, iter = 0, gsmc = 0, status = 0;
+    double gamma = 0.0, evidence = 0.0;
+    std::vector<double> parts, Ls, qs;
+};
+static const char STATE_MAGIC[8] = {'S', 'M', 'C', 'G', 'P', 'U', 'S', '1'};
+
+static bool write_state(const char *dir, const OuterState &st) {
+    const std::string path = std::string(dir) + std::to_string(st.iter) + ".state";
+    const std::string tmp = path + ".tmp";
+    FILE *f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return false;
+    bool ok = std::fwrite(STATE_MAGIC, 1, 8, f) == 8;
+    const int32_t hdr[5] = {st.nd, st.N, st.iter, st.gsmc, st.status};
+    const double sc[2] = {st.gamma, st.evidence};
+    ok = ok && std::fwrite(hdr, sizeof(int32_t), 5, f) == 5 && std::fwrite(sc, sizeof(double), 2, f) == 2;
+    ok = ok && std::fwrite(st.parts.data(), sizeof(double), st.parts.size(), f) == st.parts.size();
+    ok = ok && std::fwrite(st.Ls.data(), sizeof(double), st.Ls.size(), f) == st.Ls.size();
+    ok = ok && std::fwrite(st.qs.data(), sizeof(double), st.qs.size(), f) == st.qs.size();
+    ok = (std::fclose(f) == 0) && ok;
+    return ok && std::rename(tmp.c_str(), path.c_str()) == 0;
+}
+
+static std::string read_state(const char *path, OuterState &st) {
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return std::string("cannot open ") + path;
+    char magic[8];
+    int32_t hdr[5];
+    double sc[2];
+    std::string err;
+    if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, STATE_MAGIC, 8) != 0) err = "not an outer-SMC state file";
+    if (err.empty() && (std::fread(hdr, sizeof(int32_t), 5, f) != 5 || std::fread(sc, sizeof(double), 2, f) != 2))
+        err = "truncated header";
+    if (err.empty() && (hdr[0] < 1 || hdr[1] < 2 || hdr[2] < 0)) err = "bad header";
+    if (err.empty()) {
+        st.nd = hdr[0]; st.N = hdr[1]; st.iter = hdr[2]; st.gsmc = hdr[3]; st.status = hdr[4];
+        st.gamma = sc[0]; st.evidence = sc[1];
+        st.parts.resize((size_t)st.N * st.nd);
+        st.Ls.resize(st.N);
+        st.qs.resize(st.N);
+        if (std::fread(st.parts.data(), sizeof(double), st.parts.size(), f) != st.parts.size() ||
+            std::fread(st.Ls.data(), sizeof(double), st.Ls.size(), f) != st.Ls.size() ||
+            std::fread(st.qs.data(), sizeof(double), st.qs.size(), f) != st.qs.size())
+            err = "truncated state";
+    }
+    std::fclose(f);
+    return err;
+}
+
 static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64_t seed, const char *output_dir,
                          const GsmcQ *gq, double *particles_out, double *likelihood_out, double *evidence_out,
-                         int32_t *nstage_out) {
+                         int32_t *nstage_out, const OuterState *resume = nullptr) {
     if (!ctx) return SMCGPU_ERR_ARG;
     int r = check_ready(ctx);
     if (r) return r;
@@ -336,6 +388,25 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
         for (int q = 0; q < nb; ++q) status |= stv[q];
         return SMCGPU_OK;
     };
+    double gamma = 0.0, evidence = 0.0;
+    int iter = 1;
+    auto save_state = [&](int it) {
+        if (!output_dir) return;
+        OuterState o;
+        o.nd = nd; o.N = N; o.iter = it; o.gsmc = gq ? 1 : 0; o.status = status;
+        o.gamma = gamma; o.evidence = evidence;
+        o.parts = parts; o.Ls = Ls; o.qs = qs;
+        if (!write_state(output_dir, o)) status |= SMCGPU_ST_NONFINITE;
+    };
+    if (resume) {
+        parts = resume->parts;
+        Ls = resume->Ls;
+        qs = resume->qs;
+        gamma = resume->gamma;
+        evidence = resume->evidence;
+        iter = resume->iter + 1;
+        status = resume->status;
+    } else {
     // fault_sample_init_particles (smc_fault.f90:29-64): the prior box, or
     // N(qmean, qcov) in GSMC mode
     if (gq) {
@@ -362,8 +433,8 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
             for (int i = 0; i < N; ++i) qs[i] = neglog_q(*gq, &parts[(size_t)i * nd], nd);
     }
     if (output_dir) write_stage_csv(output_dir, 0, parts, Ls, N, nd);
-    double gamma = 0.0, evidence = 0.0;
-    int iter = 1;
+    save_state(0);
+    }
     CU(ctx->d_w.ensure(N), "alloc");
     CU(ctx->d_counts.ensure(N), "alloc");
     CU(ctx->d_flag.ensure(1), "alloc");
@@ -509,6 +580,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
         Ls = newL;
         qs = newq;
         if (output_dir) write_stage_csv(output_dir, iter, parts, Ls, N, nd);
+        save_state(iter);
         iter = iter + 1;
         if (iter > 100000) break;
     }
@@ -525,6 +597,26 @@ extern "C" int32_t smcgpu_fault_smc_exec(smcgpu_ctx *ctx, const double *range, i
                                          double *evidence_out, int32_t *nstage_out) {
     return outer_smc(ctx, range, N, seed, output_dir, nullptr, particles_out, likelihood_out, evidence_out,
                      nstage_out);
+}
+
+extern "C" int32_t smcgpu_fault_smc_resume(smcgpu_ctx *ctx, const double *range, int32_t N, uint64_t seed,
+                                           const char *output_dir, const char *state_path, const double *qmean,
+                                           const double *qcov_chol, const double *qcov_inv, double log_qcov_det,
+                                           double *particles_out, double *likelihood_out, double *evidence_out,
+                                           int32_t *nstage_out) {
+    if (!ctx) return SMCGPU_ERR_ARG;
+    if (!state_path) return ctx->fail(SMCGPU_ERR_ARG, "fault_smc_resume: state_path missing");
+    OuterState st;
+    std::string e = read_state(state_path, st);
+    if (!e.empty()) return ctx->fail(SMCGPU_ERR_ARG, "fault_smc_resume: " + e);
+    if (st.nd != ctx->mesh.ndim_fault || st.N != N)
+        return ctx->fail(SMCGPU_ERR_ARG, "fault_smc_resume: state has a different ndim_fault or nparticle");
+    const bool has_q = qmean && qcov_chol && qcov_inv;
+    if ((st.gsmc != 0) != has_q)
+        return ctx->fail(SMCGPU_ERR_ARG, "fault_smc_resume: GSMC parameters must be given exactly for a GSMC state");
+    GsmcQ q{qmean, qcov_chol, qcov_inv, log_qcov_det};
+    return outer_smc(ctx, range, N, seed, output_dir, has_q ? &q : nullptr, particles_out, likelihood_out,
+                     evidence_out, nstage_out, &st);
 }
 
 extern "C" int32_t smcgpu_fault_smc_exec_gsmc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64_t seed,

@@ -262,3 +262,40 @@ def test_outer_smc_gsmc_matches_oracle(smcgpu, orc):
     # the uniform-prior run differs: the mode switch is live
     p2, l2, ev2, ns2 = g.fault_smc_exec(rg, 24, 6)
     assert ev2 != ev
+
+
+@pytest.mark.parametrize("mode", ["uniform", "gsmc"])
+def test_outer_smc_resume_equals_uninterrupted(smcgpu, orc, tmp_path, mode):
+    """fault_smc_exec writes <k>.state after every stage; a run continued
+    from stage 2 ends with the same stages, evidence and population as the
+    uninterrupted run (every draw is keyed by its stage)."""
+    w, obs, o = setup_case("tiny", orc, nparticle=32)
+    w.settings.ntau = 1
+    w.settings.cv_outer = 1.0
+    from smc_inversion_fort_gb300.configs import prior_range
+    rg = prior_range(w)
+    rg[3] = [20.0, 28.0]
+    rg[5] = [0.0, 60.0]
+    gq = None
+    if mode == "gsmc":
+        qmean = 0.5 * (rg[:, 0] + rg[:, 1])
+        qcov = np.diag((0.15 * (rg[:, 1] - rg[:, 0]) + 1e-3) ** 2)
+        gq = {"qmean": qmean, "qcov_chol": np.linalg.cholesky(qcov), "qcov_inv": np.linalg.inv(qcov),
+              "log_qcov_det": float(np.linalg.slogdet(qcov)[1])}
+    g = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
+    g.set_data(obs)
+    d1 = str(tmp_path / "run1") + "/"
+    parts, lik, ev, ns = g.fault_smc_exec(rg, 24, 7, output_dir=d1, gsmc=gq)
+    assert ns >= 3
+    import os
+    for k in range(ns + 1):
+        assert os.path.exists(d1 + f"{k}.state") and os.path.exists(d1 + f"{k}.csv")
+    d2 = str(tmp_path / "run2") + "/"
+    p2, l2, ev2, ns2 = g.fault_smc_resume(rg, 24, 7, d1 + "2.state", output_dir=d2, gsmc=gq)
+    assert ns2 == ns and ev2 == ev
+    np.testing.assert_array_equal(p2, parts)
+    np.testing.assert_array_equal(l2, lik)
+    assert open(d1 + f"{ns}.csv").read() == open(d2 + f"{ns}.csv").read()
+    with pytest.raises(smcgpu.SmcError):
+        g.fault_smc_resume(rg, 24, 7, d1 + "2.state", gsmc=None if gq else {"qmean": rg[:, 0], "qcov_chol": np.eye(len(rg)),
+                                                                           "qcov_inv": np.eye(len(rg)), "log_qcov_det": 0.0})
