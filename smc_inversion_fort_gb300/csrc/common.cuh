@@ -83,12 +83,40 @@ __device__ __forceinline__ double rng_normal(uint64_t seed, uint64_t stream, uin
     return sqrt(-2.0 * log(r)) * sin(2.0 * pi * s);
 }
 
+// FP32 uniform from the top 23 bits of a raw word, clipped like
+// random_number_correction: integer and FP32 operations only
+__device__ __forceinline__ float clip_uniform_f(uint64_t raw) {
+    const float u = __uint_as_float(0x3F800000u | (uint32_t)(raw >> 41)) - 1.0f;
+    return u < 1e-5f ? 1e-5f : u;
+}
+
+// MIXED normals: the same Philox blocks as rng_normal, FP32 arithmetic
 __device__ __forceinline__ float rng_normal_f(uint64_t seed, uint64_t stream, uint32_t purpose, uint32_t stage,
                                               uint64_t i, uint64_t d) {
     U64x4 o = philox4x64(((uint64_t)stage << 32) | purpose, i, d >> 1, 0, seed, stream);
     int b = (int)(d & 1) * 2;
-    float r = (float)clip_uniform(o.v[b]), s = (float)clip_uniform(o.v[b + 1]);
+    float r = clip_uniform_f(o.v[b]), s = clip_uniform_f(o.v[b + 1]);
     return sqrtf(-2.0f * __logf(r)) * __sinf(6.2831853f * s);
+}
+// both normals of one block: dimensions 2k and 2k+1
+__device__ __forceinline__ float2 rng_normal2_f(uint64_t seed, uint64_t stream, uint32_t purpose, uint32_t stage,
+                                                uint64_t i, uint64_t k) {
+    U64x4 o = philox4x64(((uint64_t)stage << 32) | purpose, i, k, 0, seed, stream);
+    const float r0 = clip_uniform_f(o.v[0]), s0 = clip_uniform_f(o.v[1]);
+    const float r1 = clip_uniform_f(o.v[2]), s1 = clip_uniform_f(o.v[3]);
+    return make_float2(sqrtf(-2.0f * __logf(r0)) * __sinf(6.2831853f * s0),
+                       sqrtf(-2.0f * __logf(r1)) * __sinf(6.2831853f * s1));
+}
+
+// exact FP32 value of a double that holds an FP32 number (MIXED particle
+// values), by integer operations; other values fall back to a conversion
+__device__ __forceinline__ float f32_of_f32valued(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const uint32_t hi = (uint32_t)(b >> 32);
+    const int e = (int)((hi >> 20) & 0x7FF);
+    if (e >= 897 && e <= 1150 && (b & 0x1FFFFFFFull) == 0)
+        return __uint_as_float((hi & 0x80000000u) | ((uint32_t)(e - 896) << 23) | (uint32_t)((b >> 29) & 0x7FFFFF));
+    return (b << 1) == 0 ? __uint_as_float(hi & 0x80000000u) : (float)v;
 }
 
 // random_number_correction_dd: binary128 uniform carried as an exact 106-bit

@@ -53,7 +53,7 @@ struct smcgpu_ctx {
     smc::DevBuf<int> d_status;
     smc::DevBuf<unsigned long long> d_streams;
     smc::DevBuf<double> d_parts, d_parts_new, d_dbuf, d_trace;
-    smc::DevBuf<float> d_A32;
+    smc::DevBuf<float> d_A32, d_lv32, d_ll32;
     smc::DevBuf<int> d_ibuf, d_nstage_tmp, d_nstage;
     smc::DevBuf<double> d_w;
     smc::DevBuf<int> d_counts, d_flag;

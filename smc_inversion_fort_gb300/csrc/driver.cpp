@@ -70,6 +70,8 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
     CU(ctx->d_dbuf.ensure((size_t)chunk * 9 * N), "alloc dbuf");
     CU(ctx->d_ibuf.ensure((size_t)chunk * 4 * NP2), "alloc ibuf");
     CU(ctx->d_A32.ensure((size_t)chunk * D * D), "alloc A32");
+    CU(ctx->d_lv32.ensure((size_t)chunk * std::max(pm.nrow, 1) * 9), "alloc lv32");
+    CU(ctx->d_ll32.ensure((size_t)chunk * std::max<size_t>(pm.ll_col.size(), 1)), "alloc ll32");
     CU(ctx->d_nstage_tmp.ensure((size_t)chunk), "alloc");
     for (int t0 = 0; t0 < n; t0 += chunk) {
         int nb = std::min(chunk, n - t0);
@@ -98,6 +100,8 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
         CU(smc::launch_gibbs(ctx->md, a, s), "gibbs kernel");
         const char *why = nullptr;
         a.A32 = ctx->d_A32.p;
+        a.lv32 = ctx->d_lv32.p;
+        a.ll32 = ctx->d_ll32.p;
         a.warps_per_theta = ctx->cfg.inner_warps;
         a.engine = ctx->cfg.inner_engine;
         cudaError_t e = smc::launch_inner(ctx->md, a, s, &why);

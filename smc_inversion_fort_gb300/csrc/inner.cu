@@ -122,15 +122,57 @@ __device__ __forceinline__ double dd_div_into_w(double w, dd s) {
     double r = fma(-q, s.hi, w) - q * s.lo;
     return q + r / s.hi;
 }
+// Reflection into [0, max_slip] with momentum flips (smc_slip.f90:787-799).
+// The loop body runs once as predicated selects (a no-op inside the box, so
+// the result equals the reference's loop), and the loop proper only for the
+// rare multiple reflection: no divergent branch on the common path.
 template <typename T>
 __device__ __forceinline__ void reflect_w(T &x, T &p, T mx, int &flag) {
-    int it = 0;
-    while (x < T(0) || x > mx) {
-        if (x > mx) { x = T(2) * mx - x; p = -p; }
-        if (x < T(0)) { x = -x; p = -p; }
-        if (++it > 1000000) { flag |= SMCGPU_ST_REFLECT_CAP; break; }
+    const bool h = x > mx;
+    x = h ? T(2) * mx - x : x;
+    p = h ? -p : p;
+    const bool l = x < T(0);
+    x = l ? -x : x;
+    p = l ? -p : p;
+    if (x < T(0) || x > mx) {
+        int it = 1;
+        while (x < T(0) || x > mx) {
+            if (x > mx) { x = T(2) * mx - x; p = -p; }
+            if (x < T(0)) { x = -x; p = -p; }
+            if (++it > 1000000) { flag |= SMCGPU_ST_REFLECT_CAP; break; }
+        }
     }
 }
+// Blow-up test (|x| > 1e3 freezes the chain and rejects it,
+// smc_slip.f90:800-806) and reflection, branch-free unless either fires
+template <typename T>
+__device__ __forceinline__ bool blow_or_reflect(T &x, T &p, T mx, int &flag) {
+    const bool blow = (x < T(0) ? -x : x) > T(1e3);   // |x| in T itself (no promotion)
+    T xr = x, pr = p;
+    reflect_w<T>(xr, pr, mx, flag);
+    x = blow ? x : xr;
+    p = blow ? p : pr;
+    return blow;
+}
+// MIXED reflection in closed form: the reference's loop folds x into
+// [0, max_slip] by successive reflections at 0 and max_slip (a triangle wave
+// of period 2 max_slip) and flips p once per reflection.  For |x| well
+// beyond max_slip (the tuning pass draws step sizes up to 1) the loop runs
+// |x|/max_slip times; here the fold and the parity of the reflection count
+// are computed directly.  Same map up to rounding; entries inside the box
+// are unchanged.  imx = 1/max_slip.
+__device__ __forceinline__ void reflect_fold(float &x, float &p, float mx, float imx) {
+    const bool neg = x < 0.0f, out = neg || x > mx;
+    const float u = (neg ? -x : x) * imx;
+    const float k = fmaxf(ceilf(u) - 1.0f, 0.0f);   // reflections after the first one of a negative x
+    const float fr = u - k;                          // in (0, 1]
+    const int ki = (int)k;
+    const float xf = (ki & 1) ? (1.0f - fr) * mx : fr * mx;
+    const int flips = ki + (neg ? 1 : 0);
+    x = out ? xf : x;
+    p = (out && (flips & 1)) ? -p : p;
+}
+
 // Sum of 16 per-slot values over the 32 lanes of a warp: afterwards lane l
 // holds the total of slot l >> 1 (in v[0]); 16 exchanges instead of 80.
 __device__ __forceinline__ double wreduce16(double v[16], int lane) {
@@ -311,7 +353,7 @@ struct Layout {
     }
     __host__ __device__ static int slots(int W) { return ENG == ENG_CC ? W * CW : S; }
     __host__ __device__ static size_t bytes(int W) {
-        size_t b = engine_bytes(W) + (size_t)4 * DP * sizeof(T) + (size_t)6 * DP * sizeof(double) +
+        size_t b = engine_bytes(W) + (size_t)7 * DP * sizeof(T) + (size_t)6 * DP * sizeof(double) +
                    (size_t)slots(W) * (5 * sizeof(double) + 5 * sizeof(int)) + (size_t)(4 * W + 8) * sizeof(double);
         if (ENG != ENG_CC) b += (size_t)5 * 32 * (W > 4 ? W : 4) * sizeof(double) + 64;   // reductions, masks, mbarrier
         return (b + 127) & ~(size_t)127;
@@ -357,7 +399,8 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
     }
     sp += L_::engine_bytes(W);
     T *tcov = (T *)sp, *tmean = tcov + DP, *tcv = tmean + DP, *tisc = tcv + DP;
-    double *vb = (double *)(tisc + DP);
+    T *tvg = tisc + DP, *tvh = tvg + DP, *ticov = tvh + DP;   // MIXED end-point terms in T
+    double *vb = (double *)(ticov + DP);
     double *vcov = vb + DP, *vmean = vcov + DP, *vg = vmean + DP, *vh = vg + DP, *vc = vh + DP;
     double *sdall = vc + DP;                                   // NS * 5 doubles
     int *siall = (int *)(sdall + (size_t)NS * 5);              // NS * 5 ints
@@ -400,11 +443,16 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
     }
     for (int i = gt; i < DP; i += gnt) vb[i] = i < D ? bth[i] : 0.0;
     for (int k = gt; k < N; k += gnt) dtau[k] = exp(-5.0);
+    float *lv32 = a.lv32 ? a.lv32 + (size_t)th * m.nrow * 9 : nullptr;
+    float *ll32 = a.ll32 ? a.ll32 + (size_t)th * m.ll_nnz : nullptr;
+    float *wf = (float *)(Lc + 8 * N);   // MIXED: FP32 copy of the normalised weights
     if constexpr (ENG == ENG_MMA) {
         for (int e = gt; e < DP * DP; e += gnt) {
             const int k = e / DP, r = e % DP;
             tA32[e] = (k < D && r < D) ? (float)Ath[(size_t)k * D + r] : 0.0f;
         }
+        for (int e = gt; e < m.nrow * 9; e += gnt) lv32[e] = (float)lv[e];
+        for (int e = gt; e < m.ll_nnz; e += gnt) ll32[e] = (float)llv[e];
     } else if (MIXED) {
         for (int e = gt; e < D * D; e += gnt) A32[e] = (float)Ath[e];
     }
@@ -480,9 +528,8 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                     ps2 = fmaf(wk, wk, ps2);
                 }
                 grp.sum2f(ps, ps2);
-                double s1 = ps, s2 = ps2;
-                double mean = s1 / N;
-                cv = sqrt(fmax(s2 / N - mean * mean, 0.0)) / mean;
+                const float invn = 1.0f / (float)N, meanf = ps * invn;
+                cv = (double)(sqrtf(fmaxf(ps2 * invn - meanf * meanf, 0.0f)) / meanf);
             } else {
                 double ps = 0.0;
                 for (int k = gt; k < N; k += gnt) {
@@ -528,9 +575,42 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
             dd p2 = {0.0, 0.0};
             for (int k = gt; k < N; k += gnt) p2 = dd_add_d(p2, w[k]);
             dd sw = grp.sum_dd(p2);
-            for (int k = gt; k < N; k += gnt) w[k] = dd_div_into_w(w[k], sw);
+            for (int k = gt; k < N; k += gnt) {
+                w[k] = dd_div_into_w(w[k], sw);
+                if (MIXED) wf[k] = (float)w[k];
+            }
             grp.sync();
         }
+        if constexpr (MIXED && ENG != ENG_CC) {
+            // thread (d, kp) sums particles k = kp, kp + KP, ...; partials in FP32
+            const int KP = gnt / DP, d = gt % DP, kp = gt / DP;
+            float *fs = (float *)red;
+            float md = 0.0f;
+            if (kp < KP && d < D)
+                for (int k = kp; k < N; k += KP) md = fmaf(wf[k], f32_of_f32valued(parts[(size_t)k * D + d]), md);
+            fs[gt] = md;
+            grp.sync();
+            if (gt < DP) {
+                float t = 0.0f;
+                for (int q = 0; q < KP; ++q) t += fs[q * DP + gt];
+                vmean[gt] = gt < D ? (double)t : 0.0;
+            }
+            grp.sync();
+            const float mu = (float)vmean[d];
+            float cd = 0.0f;
+            if (kp < KP && d < D)
+                for (int k = kp; k < N; k += KP) {
+                    const float di = f32_of_f32valued(parts[(size_t)k * D + d]) - mu;
+                    cd = fmaf(wf[k] * di, di, cd);
+                }
+            fs[gt] = cd;
+            grp.sync();
+            if (gt < DP) {
+                float t = 0.0f;
+                for (int q = 0; q < KP; ++q) t += fs[q * DP + gt];
+                vcov[gt] = gt >= D ? 1.0 : (fabsf(t) < 1e-3f ? 1e-3 : (double)t);
+            }
+        } else
         for (int d = gt; d < DP; d += gnt) {
             if (d >= D) { vmean[d] = 0.0; vcov[d] = 1.0; continue; }
             if (!MIXED) {
@@ -574,20 +654,25 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
         }
         // ---- stage matrix
         if constexpr (ENG == ENG_MMA) {
-            // M row i split into BF16 hi + lo, row-major with row stride DP+8
-            for (int i = gt; i < DP; i += gnt) {
+            // M = gamma A + L^T L / alpha^2 in FP32 (A from the FP32 copy in shared
+            // memory), split into BF16 hi + lo, row-major with row stride DP+8;
+            // TPR threads per row, KC consecutive columns each
+            const float gf = (float)gamma, ia2 = (float)(1.0 / alpha2);
+            const int TPR = gnt / DP, KC = DP / TPR;
+            for (int q = gt; q < DP * TPR; q += gnt) {
+                const int i = q / TPR, k0 = (q % TPR) * KC;
                 int e = i < D ? m.ll_ptr[i] : 0;
                 const int e1 = i < D ? m.ll_ptr[i + 1] : 0;
+                while (e < e1 && m.ll_col[e] < k0) ++e;
                 __nv_bfloat16 *rh = (__nv_bfloat16 *)Ahi + (size_t)i * L_::AST;
                 __nv_bfloat16 *rl = (__nv_bfloat16 *)Alo + (size_t)i * L_::AST;
-                for (int k = 0; k < DP; ++k) {
-                    double v = 0.0;
+                for (int k = k0; k < k0 + KC; ++k) {
+                    float v = 0.0f;
                     if (i < D && k < D) {
-                        v = gamma * Ath[(size_t)k * D + i];
-                        while (e < e1 && m.ll_col[e] < k) ++e;
-                        if (e < e1 && m.ll_col[e] == k) v += llv[e] / alpha2;
+                        v = gf * tA32[k * DP + i];
+                        if (e < e1 && m.ll_col[e] == k) { v += ll32[e] * ia2; ++e; }
                     }
-                    tc::split_bf16((float)v, rh[k], rl[k]);
+                    tc::split_bf16(v, rh[k], rl[k]);
                 }
             }
         } else if constexpr (TC) {
@@ -658,6 +743,9 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
             tmean[i] = (T)vmean[i];
             tcv[i] = MIXED ? (T)vc[i] : (T)(gamma * vb[i]);
             tisc[i] = (T)(1.0 / sqrt(vcov[i]));
+            tvg[i] = (T)vg[i];
+            tvh[i] = (T)vh[i];
+            ticov[i] = (T)(1.0 / vcov[i]);
         }
         grp.sync();
 
@@ -728,6 +816,7 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                         live_l[aa][h] = r < D;
                     }
                 float x[MTW][NTW][4], p[MTW][NTW][4], dts[NTW][2];
+                const float imx = 1.0f / (float)mx;
                 // this warp's rows of M as A fragments (hi, lo): held in registers
                 // for the whole pass when they are few, else loaded every step
                 constexpr bool AREG = MTW * KT <= 4;
@@ -803,19 +892,26 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                     if (frm != 0ull)
                         for (int e = gt; e < S * DP; e += NTH) {
                             const int c = e / DP, r = e % DP;
-                            if ((frm >> c) & 1ull) tXC[r * TS + c] = r < D ? (float)parts[(size_t)spar[c] * D + r] : 0.0f;
+                            if ((frm >> c) & 1ull) tXC[r * TS + c] = r < D ? f32_of_f32valued(parts[(size_t)spar[c] * D + r]) : 0.0f;
                         }
-                    double kin = 0.0;
+                    float kin = 0.0f;
                     {
+                        // dimensions in pairs: one Philox block gives both normals
                         const bool on = (actm >> cs) & 1ull;
                         const int jj = sj[cs];
-                        for (int r = part; r < DP; r += NPART) {
-                            float pv = 0.0f;
-                            if (on && r < D) {
-                                pv = rng_normal_f(a.seed, stream, P_MOM, iter, jj, r) * (float)tisc[r];
-                                kin += (double)(pv * (float)tcov[r] * pv * 0.5f);
+                        for (int r0 = 2 * part; r0 < DP; r0 += 2 * NPART) {
+                            float p0 = 0.0f, p1 = 0.0f;
+                            if (on && r0 < D) {
+                                const float2 z = rng_normal2_f(a.seed, stream, P_MOM, iter, jj, (uint64_t)(r0 >> 1));
+                                p0 = z.x * (float)tisc[r0];
+                                kin += p0 * (float)tcov[r0] * p0 * 0.5f;
+                                if (r0 + 1 < D) {
+                                    p1 = z.y * (float)tisc[r0 + 1];
+                                    kin += p1 * (float)tcov[r0 + 1] * p1 * 0.5f;
+                                }
                             }
-                            tP[r * TS + cs] = pv;
+                            tP[r0 * TS + cs] = p0;
+                            tP[(r0 + 1) * TS + cs] = p1;
                         }
                     }
                     grp.sync();
@@ -825,6 +921,18 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                         dts[bb][0] = (float)sdt[c0];
                         dts[bb][1] = (float)sdt[c0 + 1];
                     }
+                    bool on[MTW][NTW][4];
+                    float cdt[MTW][NTW][4];
+#pragma unroll
+                    for (int aa = 0; aa < MTW; ++aa)
+#pragma unroll
+                        for (int bb = 0; bb < NTW; ++bb)
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                const int c = 8 * (nt0 + bb) + 2 * t4 + (e & 1);
+                                on[aa][bb][e] = live_l[aa][e >> 1] && ((actm >> c) & 1ull);
+                                cdt[aa][bb][e] = cov_l[aa][e >> 1] * dts[bb][e & 1];
+                            }
 #pragma unroll
                     for (int aa = 0; aa < MTW; ++aa)
 #pragma unroll
@@ -886,7 +994,14 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                             for (int bb = 0; bb < NTW; ++bb)
 #pragma unroll
                                 for (int e = 0; e < 4; ++e) acc[aa][bb][e] += acc1[aa][bb][e] + acc2[aa][bb][e];
-                        const float hstep = it == 0 ? 0.5f : 1.0f, xstep = it == a.ntau ? 0.5f : 1.0f;
+                        // momentum and position updates with the step factors of this
+                        // step; the reflection / blow-up path only for entries that left
+                        // [0, max_slip]; chains that blew up stay frozen
+                        const float hs = it == 0 ? 0.5f : 1.0f, xs = it == a.ntau ? 0.5f : 1.0f;
+                        // common step: update and one range test; entries that left the
+                        // box (reflection, or |x| > 1e3: the chain blows up) go through a
+                        // warp-uniform branch
+                        unsigned outmask = 0u;
 #pragma unroll
                         for (int aa = 0; aa < MTW; ++aa)
 #pragma unroll
@@ -894,15 +1009,30 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
 #pragma unroll
                                 for (int e = 0; e < 4; ++e) {
                                     const int h = e >> 1, c = 8 * (nt0 + bb) + 2 * t4 + (e & 1);
-                                    if (live_l[aa][h] && ((actm >> c) & 1ull) && !((blm >> c) & 1ull)) {
-                                        const float gr = cv_l[aa][h] + acc[aa][bb][e];
-                                        const float dt = dts[bb][e & 1];
-                                        p[aa][bb][e] = p[aa][bb][e] - gr * hstep * dt;
-                                        x[aa][bb][e] = x[aa][bb][e] + cov_l[aa][h] * p[aa][bb][e] * xstep * dt;
-                                        if (fabsf(x[aa][bb][e]) > 1e3f) atomicOr(&masks[2], 1ull << c);
-                                        else reflect_w<float>(x[aa][bb][e], p[aa][bb][e], mx, flag);
-                                    }
+                                    bool live = on[aa][bb][e];
+                                    if (blm != 0ull) live = live && !((blm >> c) & 1ull);
+                                    const float gr = cv_l[aa][h] + acc[aa][bb][e];
+                                    const float pn = p[aa][bb][e] - gr * (hs * dts[bb][e & 1]);
+                                    const float xn = x[aa][bb][e] + cdt[aa][bb][e] * xs * pn;
+                                    x[aa][bb][e] = live ? xn : x[aa][bb][e];
+                                    p[aa][bb][e] = live ? pn : p[aa][bb][e];
+                                    const bool out = !(xn >= 0.0f && xn <= mx);
+                                    outmask |= (live && out) ? 1u << ((aa * NTW + bb) * 4 + e) : 0u;
                                 }
+                        if (__any_sync(FULL, outmask != 0u)) {
+#pragma unroll
+                            for (int aa = 0; aa < MTW; ++aa)
+#pragma unroll
+                                for (int bb = 0; bb < NTW; ++bb)
+#pragma unroll
+                                    for (int e = 0; e < 4; ++e) {
+                                        if (!((outmask >> ((aa * NTW + bb) * 4 + e)) & 1u)) continue;
+                                        const int c = 8 * (nt0 + bb) + 2 * t4 + (e & 1);
+                                        float &xe = x[aa][bb][e];
+                                        if ((xe < 0.0f ? -xe : xe) > 1e3f) atomicOr(&masks[2], 1ull << c);
+                                        else reflect_fold(xe, p[aa][bb][e], mx, imx);
+                                    }
+                        }
                         if (it < a.ntau) {
                             write_b((it + 1) & 1);
                         } else {
@@ -928,7 +1058,9 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                     // kinetic energy, tuning distance (partial over this thread's dimensions)
                     const unsigned long long blm = masks[2];
                     const float *dl = (const float *)(Bhi + 2 * (size_t)((a.ntau + 1) & 1) * L_::B_BYTES);
-                    double q0 = 0.0, q1 = 0.0, q2 = 0.0, q3 = 0.0;
+                    // FP32 per-thread partial sums: the expansion point (the stage
+                    // mean) is FP32-exact, so these are offsets from L(sbar), P(sbar)
+                    float q0 = 0.0f, q1 = 0.0f, q2 = 0.0f, q3 = 0.0f;
                     if ((actm >> cs) & 1ull) {
                         // rows part + i NPART of A times the offsets: RPT independent chains
                         constexpr int RPT = DP / NPART;
@@ -945,58 +1077,55 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                         for (int i = 0; i < RPT; ++i) {
                             const int r = part + i * NPART;
                             if (r >= D) continue;
-                            const double ic = 1.0 / vcov[r];
-                            const double del = (double)tX[r * TS + cs] - vmean[r];
-                            q0 += vg[r] * del + 0.5 * (double)dl[r * TS + cs] * (double)af[i];
-                            q1 += vh[r] * del;
-                            const double pr = (double)tP[r * TS + cs];
-                            q2 += 0.5 * pr * vcov[r] * pr;
-                            const double dx = (double)tX[r * TS + cs] - (double)tXC[r * TS + cs];
-                            q3 += dx * dx * ic;
+                            const float dr = dl[r * TS + cs];
+                            q0 += (float)tvg[r] * dr + 0.5f * dr * af[i];
+                            q1 += (float)tvh[r] * dr;
+                            const float pr = tP[r * TS + cs];
+                            q2 += 0.5f * pr * (float)tcov[r] * pr;
+                            const float dx = tX[r * TS + cs] - tXC[r * TS + cs];
+                            q3 += dx * dx * (float)ticov[r];
                         }
-                        const double i2a = 1.0 / (2.0 * alpha2);
+                        const float i2a = (float)(1.0 / (2.0 * alpha2));
                         for (int r2 = part; r2 < m.nrow; r2 += NPART) {
-                            int cl[9];
-                            double lw[9];
+                            float tt = 0.0f;
 #pragma unroll
                             for (int k9 = 0; k9 < 9; ++k9) {
-                                cl[k9] = __ldg(m.l_col + r2 * 9 + k9);
-                                lw[k9] = __ldg(lv + (size_t)r2 * 9 + k9);
+                                const int cl = __ldg(m.l_col + r2 * 9 + k9);
+                                if (cl >= 0) tt = fmaf(__ldg(lv32 + r2 * 9 + k9), dl[cl * TS + cs], tt);
                             }
-                            double tt = 0.0;
-#pragma unroll
-                            for (int k9 = 0; k9 < 9; ++k9)
-                                if (cl[k9] >= 0) tt += lw[k9] * (double)dl[cl[k9] * TS + cs];
                             q1 += tt * tt * i2a;
                         }
                     }
-                    red[0 * NTH + part * S + cs] = q0;
-                    red[1 * NTH + part * S + cs] = q1;
-                    red[2 * NTH + part * S + cs] = q2;
-                    red[3 * NTH + part * S + cs] = q3;
-                    red[4 * NTH + part * S + cs] = kin;
+                    float *redf = (float *)red;
+                    redf[0 * NTH + part * S + cs] = q0;
+                    redf[1 * NTH + part * S + cs] = q1;
+                    redf[2 * NTH + part * S + cs] = q2;
+                    redf[3 * NTH + part * S + cs] = q3;
+                    redf[4 * NTH + part * S + cs] = kin;
                     grp.sync();
                     // Metropolis test and bookkeeping (smc_slip.f90:695-716, 1057-1094)
                     if (gt < 64) {
                         const int c = gt;
                         bool accd = false;
                         if (c < S && ((actm >> c) & 1ull)) {
-                            double q5[5];
+                            const float *redf = (const float *)red;
+                            float q5[5];
 #pragma unroll
                             for (int q = 0; q < 5; ++q) {
-                                double tt = 0.0;
-                                for (int pt = 0; pt < NPART; ++pt) tt += red[q * NTH + pt * S + c];
+                                float tt = 0.0f;
+                                for (int pt = 0; pt < NPART; ++pt) tt += redf[q * NTH + pt * S + c];
                                 q5[q] = tt;
                             }
                             const int jj = sj[c];
                             const bool blown = (blm >> c) & 1ull;
-                            const double Lx = q5[0] + Lbar, Px = q5[1] + Pbar;
+                            const double Lx = (double)q5[0] + Lbar, Px = (double)q5[1] + Pbar;
                             const double post = gamma * Lx + Px;
-                            const double ham = blown ? 1e20 : post + q5[2];
-                            const double dham = (spost[c] + q5[4]) - ham;
-                            if (tuning) score[jj] = blown ? 0.0 : q5[3] * exp(fmin(0.0, dham));
+                            const double ham = blown ? 1e20 : post + (double)q5[2];
+                            const double dham = (spost[c] + (double)q5[4]) - ham;
+                            const float dhf = (float)fmax(dham, -1e30);
+                            if (tuning) score[jj] = blown ? 0.0 : (double)(q5[3] * expf(fminf(0.0f, dhf)));
                             const double u = rng_uniform(a.seed, stream, P_MH, iter, jj, 0);
-                            if (!blown && dham > log(u)) {
+                            if (!blown && dhf > logf((float)u)) {
                                 accd = true;
                                 sL[c] = Lx;
                                 sP[c] = Px;
@@ -1128,8 +1257,9 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                                 const float gr = cv_r + acc[s];
                                 p[s] = p[s] - gr * hstep * dts[s];
                                 x[s] = x[s] + cov_r * p[s] * xstep * dts[s];
-                                if (fabsf(x[s]) > 1e3f) atomicOr(&masks[2], 1ull << c);
-                                else reflect_w<float>(x[s], p[s], mx, flag);
+                                const bool blow = (x[s] < 0.0f ? -x[s] : x[s]) > 1e3f;
+                                if (blow) atomicOr(&masks[2], 1ull << c);
+                                else reflect_fold(x[s], p[s], mx, 1.0f / mx);
                             }
                             const float dl = rowlive ? x[s] - mean_r : 0.0f;
                             if (it < a.ntau) {
@@ -1264,6 +1394,7 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                 if (lane < CW) { sj[lane] = 0; sjend[lane] = 0; spar[lane] = -1; }
                 grp.sync();
                 T xc[RT][CTW], x[RT][CTW], p[RT][CTW], acc[RT][CTW];
+                const float imxf = 1.0f / (float)mx;
 #pragma unroll
                 for (int i = 0; i < RT; ++i)
 #pragma unroll
@@ -1356,8 +1487,13 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                                     T gr = MIXED ? tcv[r] + acc[i][q] : acc[i][q] - tcv[r];
                                     p[i][q] = p[i][q] - gr * hstep * dts[q];
                                     x[i][q] = x[i][q] + tcov[r] * p[i][q] * xstep * dts[q];
-                                    if (fabs(x[i][q]) > T(1e3)) atomicOr(&sblown[c], 1);
-                                    else reflect_w<T>(x[i][q], p[i][q], mx, flag);
+                                    if constexpr (MIXED) {
+                                        const bool blow = (x[i][q] < T(0) ? -x[i][q] : x[i][q]) > T(1e3);
+                                        if (blow) atomicOr(&sblown[c], 1);
+                                        else reflect_fold(x[i][q], p[i][q], mx, imxf);
+                                    } else if (blow_or_reflect<T>(x[i][q], p[i][q], mx, flag)) {
+                                        atomicOr(&sblown[c], 1);
+                                    }
                                 }
                                 Xw[r * CW + c] = (r < D) ? (MIXED ? x[i][q] - tmean[r] : x[i][q]) : T(0);
                             }

@@ -20,6 +20,8 @@ struct InnerArgs {
     // per-theta operator data
     const double *A;      // [th][D][D] column-major Gram matrix
     float *A32;           // [th][D][D] FP32 copy (MIXED), written by the inner kernel
+    float *lv32;          // [th][nrow][9] FP32 copy of the L values (MIXED), written by the inner kernel
+    float *ll32;          // [th][ll_nnz] FP32 copy of the L^T L values (MIXED), written by the inner kernel
     const double *b;      // [th][D]
     const double *dsd;    // [th]
     const double *lval;   // [th][nrow][9] values of L (columns in MeshDev::l_col)
