@@ -1,5 +1,7 @@
 // Truncated-normal Gibbs initialisation of the inner population
 // (slip_gen_init_particles, smc_slip.f90:184-264).
+#include <algorithm>
+
 #include "common.cuh"
 #include "inner.h"
 
@@ -114,14 +116,100 @@ __global__ void gibbs_kernel(MeshDev m, InnerArgs a) {
     if (lane == 0 && stat) atomicOr(a.status + th, stat);
 }
 
+// MIXED: the same sweep in FP32 with the geometry's L^T L rows cached in
+// shared memory (off-diagonal columns and values, the diagonal, the
+// conditional standard deviation), so that a component update is one
+// shared-memory gather per lane, a warp sum and lane 0's inverse CDF.
+__global__ void gibbs_mixed_kernel(MeshDev m, InnerArgs a, int maxrow) {
+    extern __shared__ __align__(16) unsigned char gsm[];
+    const int wpb = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int th = blockIdx.x * wpb + wid;
+    if (th >= a.n_theta) return;
+    const int D = a.D, N = a.N, D2 = (D + 1) & ~1;
+    const size_t per = (size_t)D * maxrow * 8 + (size_t)(2 * D2 + 2 * D) * 4;
+    unsigned char *base = gsm + (size_t)wid * ((per + 15) & ~(size_t)15);
+    int *rc = (int *)base;                          // [D][maxrow] off-diagonal columns (-1: none)
+    float *rv = (float *)(rc + (size_t)D * maxrow); // [D][maxrow] values
+    float *cur = rv + (size_t)D * maxrow, *vn = cur + D2, *ilii = vn + D2, *sgr = ilii + D;
+    const float alpha2 = (float)a.aux[th].alpha2, mxs = (float)a.max_slip;
+    const double *ll = a.llval + (size_t)th * m.ll_nnz;
+    const uint64_t stream = a.streams[th];
+    double *parts = a.parts + (size_t)th * N * D;
+    for (int i = lane; i < D; i += 32) {
+        float lii = 0.0f;
+        int q = 0;
+        for (int e = m.ll_ptr[i]; e < m.ll_ptr[i + 1]; ++e) {
+            const int j = m.ll_col[e];
+            if (j == i) {
+                lii += (float)ll[e];
+            } else {
+                rc[(size_t)i * maxrow + q] = j;
+                rv[(size_t)i * maxrow + q] = (float)ll[e];
+                ++q;
+            }
+        }
+        for (; q < maxrow; ++q) { rc[(size_t)i * maxrow + q] = -1; rv[(size_t)i * maxrow + q] = 0.0f; }
+        ilii[i] = 1.0f / lii;
+        sgr[i] = sqrtf(alpha2 / lii);
+        cur[i] = 0.0f;
+    }
+    __syncwarp();
+    for (int k = 0; k < N; ++k) {
+        for (int d2 = lane; d2 < D2 / 2; d2 += 32) {
+            const float2 z = rng_normal2_f(a.seed, stream, RNG_GIBBS, 0, (uint64_t)k, (uint64_t)d2);
+            vn[2 * d2] = z.x;
+            vn[2 * d2 + 1] = z.y;
+        }
+        __syncwarp();
+        for (int i = 0; i < D; ++i) {
+            float term = 0.0f;
+            if (lane < maxrow) {
+                const int j = rc[(size_t)i * maxrow + lane];
+                if (j >= 0) term = rv[(size_t)i * maxrow + lane] * cur[j];
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+            if (lane == 0) {
+                const float muf = -term * ilii[i], sg = sgr[i];
+                const float al = (0.0f - muf) / sg, be = (mxs - muf) / sg;
+                const float u = normcdff(vn[i]);
+                float z;
+                if (al >= 0.0f) {
+                    const float qa = normcdff(-al), qb = normcdff(-be);
+                    const float q = qa - u * (qa - qb);
+                    z = q > 0.0f ? -normcdfinvf(q) : al;
+                } else {
+                    const float pa = normcdff(al), pb = normcdff(be);
+                    const float p = pa + u * (pb - pa);
+                    z = p > 0.0f ? normcdfinvf(p) : be;
+                }
+                cur[i] = fminf(fmaxf(muf + sg * z, 0.0f), mxs);
+            }
+            __syncwarp();
+        }
+        for (int d = lane; d < D; d += 32) parts[(size_t)k * D + d] = (double)cur[d];
+        __syncwarp();
+    }
+}
+
 cudaError_t launch_gibbs(const MeshDev &m, const InnerArgs &a, cudaStream_t s) {
     if (a.n_theta <= 0) return cudaSuccess;
     const int wpb = 4;
     size_t sm = (size_t)wpb * 2 * a.D * sizeof(double);
     unsigned blocks = (unsigned)((a.n_theta + wpb - 1) / wpb);
     if (a.mixed) {
-        cudaFuncSetAttribute(gibbs_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        gibbs_kernel<true><<<blocks, wpb * 32, sm, s>>>(m, a);
+        // one warp per geometry; as many per block as shared memory allows (4 at most)
+        const int maxrow = m.ll_maxrow;   // at most 32: one entry per lane
+        const int D2 = (a.D + 1) & ~1;
+        const size_t per = (((size_t)a.D * maxrow * 8 + (size_t)(2 * D2 + 2 * a.D) * 4) + 15) & ~(size_t)15;
+        int dev = 0, maxsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        const int w = (int)std::max<size_t>(1, std::min<size_t>(4, (size_t)maxsm / per));
+        const size_t smm = per * w;
+        cudaError_t e = cudaFuncSetAttribute(gibbs_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smm);
+        if (e != cudaSuccess) return e;
+        gibbs_mixed_kernel<<<(unsigned)((a.n_theta + w - 1) / w), w * 32, smm, s>>>(m, a, maxrow);
     } else {
         cudaFuncSetAttribute(gibbs_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         gibbs_kernel<false><<<blocks, wpb * 32, sm, s>>>(m, a);

@@ -144,8 +144,8 @@ def test_nested_fp64_statistics_match_oracle(smcgpu, orc):
 @pytest.mark.parametrize("engine", ["mma", "cuda", "tcgen05"])
 def test_nested_mixed_matches_fp64(smcgpu, orc, engine):
     """MIXED against FP64, for every leapfrog engine (warp-level BF16x3 MMA,
-    FP32 CUDA cores, BF16x3 tcgen05): the mean -log Z over independent
-    streams agrees within 4 standard errors (and the medians within 1 nat)."""
+    FP32 CUDA cores, BF16x3 tcgen05): the mean and the median -log Z over
+    independent streams agree within 4 standard errors."""
     w, obs, o = setup_case("tiny", orc)
     th = np.vstack([true_theta(w)[None], random_thetas(w, 3, seed=4)])
     reps = 48
@@ -169,7 +169,8 @@ def test_nested_mixed_matches_fp64(smcgpu, orc, engine):
     # a property of the reference algorithm, so the check uses the mean with
     # its standard error and the median.
     assert np.all(np.abs(a.mean(1) - b.mean(1)) < 4 * se + 1e-9)
-    assert np.all(np.abs(np.median(a, 1) - np.median(b, 1)) < 1.0)
+    # the median of n draws has standard error about 1.2533 sd / sqrt(n)
+    assert np.all(np.abs(np.median(a, 1) - np.median(b, 1)) < 4 * 1.2533 * se + 1e-9)
 
 
 def test_posterior_population(smcgpu, orc):
