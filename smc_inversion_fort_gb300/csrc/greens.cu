@@ -79,14 +79,18 @@ __global__ void planes_kernel(MeshDev m, int n_theta, const double *__restrict__
 // UB0 displacement terms (DC3Dfortran.f90:314-400, components 1-3) for unit
 // strike and dip potency, z = 0 so C = D.  Not yet divided by 2*pi.
 template <typename T>
-__device__ __forceinline__ void ub0_disp(T X, T Y, T D, T SD, T CD, T alp3, T us[3], T ud[3]);
+__device__ __forceinline__ void ub0_disp(T X, T Y, T D, T SD, T CD, T aSD, T aSC, T us[3], T ud[3]);
 
 template <>
-__device__ __forceinline__ void ub0_disp<double>(double X, double Y, double D, double SD, double CD, double alp3,
-                                                 double us[3], double ud[3]) {
-    double R = sqrt(X * X + Y * Y + D * D);
+__device__ __forceinline__ void ub0_disp<double>(double X, double Y, double D, double SD, double CD, double aSD,
+                                                 double aSC, double us[3], double ud[3]) {
+    // one reciprocal square root instead of a square root and a division
+    // (about 1 ulp; the FP64 pipe is this kernel's bound)
+    const double R2 = X * X + Y * Y + D * D;
+    const double iR = rsqrt(R2);
+    const double R = R2 * iR;
     double P = Y * CD + D * SD, Q = Y * SD - D * CD;
-    double iR = 1.0 / R, RD = R + D, iRD = 1.0 / RD;
+    double RD = R + D, iRD = 1.0 / RD;
     double iR2 = iR * iR, iR3 = iR2 * iR, iR5 = iR3 * iR2;
     double QR = 3.0 * Q * iR5;
     double D12 = iR * iRD * iRD;
@@ -98,20 +102,21 @@ __device__ __forceinline__ void ub0_disp<double>(double X, double Y, double D, d
     double FI3 = X * iR3 - FI2;
     double FI4 = -XY * D32;
     double FI5 = iR * iRD - X2 * D32;
-    us[0] = -X2 * QR - alp3 * FI1 * SD;
-    us[1] = -XY * QR - alp3 * FI2 * SD;
-    us[2] = -D * X * QR - alp3 * FI4 * SD;
-    double SC = SD * CD;
-    ud[0] = -X * P * QR + alp3 * FI3 * SC;
-    ud[1] = -Y * P * QR + alp3 * FI1 * SC;
-    ud[2] = -D * P * QR + alp3 * FI5 * SC;
+    // aSD = alp3 SD, aSC = alp3 SD CD: per-plane constants
+    us[0] = -X2 * QR - aSD * FI1;
+    us[1] = -XY * QR - aSD * FI2;
+    us[2] = -D * X * QR - aSD * FI4;
+    const double PQR = P * QR;
+    ud[0] = -X * PQR + aSC * FI3;
+    ud[1] = -Y * PQR + aSC * FI1;
+    ud[2] = -D * PQR + aSC * FI5;
 }
 
 // FP32: reciprocal square root and the cancellation-free form of
 // FI3 = X/R^3 - FI2 = X*(D*(2R+D)/(R^3 RD^2) + Y^2 D33).
 template <>
-__device__ __forceinline__ void ub0_disp<float>(float X, float Y, float D, float SD, float CD, float alp3,
-                                                float us[3], float ud[3]) {
+__device__ __forceinline__ void ub0_disp<float>(float X, float Y, float D, float SD, float CD, float aSD,
+                                                float aSC, float us[3], float ud[3]) {
     float R2 = fmaf(X, X, fmaf(Y, Y, D * D));
     float iR = rsqrtf(R2);
     float R = R2 * iR;
@@ -129,27 +134,44 @@ __device__ __forceinline__ void ub0_disp<float>(float X, float Y, float D, float
     float FI3 = X * fmaf(Y2, D33, D * tR * iR3 * iRD * iRD);
     float FI4 = -XY * D32;
     float FI5 = fmaf(-X2, D32, iR * iRD);
-    us[0] = fmaf(-X2, QR, -alp3 * FI1 * SD);
-    us[1] = fmaf(-XY, QR, -alp3 * FI2 * SD);
-    us[2] = fmaf(-D * X, QR, -alp3 * FI4 * SD);
-    float SC = SD * CD;
-    ud[0] = fmaf(-X * P, QR, alp3 * FI3 * SC);
-    ud[1] = fmaf(-Y * P, QR, alp3 * FI1 * SC);
-    ud[2] = fmaf(-D * P, QR, alp3 * FI5 * SC);
+    us[0] = fmaf(-X2, QR, -aSD * FI1);
+    us[1] = fmaf(-XY, QR, -aSD * FI2);
+    us[2] = fmaf(-D * X, QR, -aSD * FI4);
+    ud[0] = fmaf(-X * P, QR, aSC * FI3);
+    ud[1] = fmaf(-Y * P, QR, aSC * FI1);
+    ud[2] = fmaf(-D * P, QR, aSC * FI5);
 }
 
 // DC3D0 displacement at one receiver for unit strike / dip potency, with the
 // reference's guards: depth < 0 returns zero (DC3Dfortran.f90:67-70),
 // |x|,|y|,|d| < 1e-6 are snapped to zero (:71-73), R == 0 returns zero (:82-85).
 template <typename T>
-__device__ __forceinline__ bool dc3d0_disp(T x, T y, T depth, T SD, T CD, T alp3, T us[3], T ud[3]) {
+__device__ __forceinline__ bool dc3d0_disp(T x, T y, T depth, T SD, T CD, T aSD, T aSC, T us[3], T ud[3]) {
     if (depth < T(0)) return false;
     const T EPS = T(1.0e-6);
     if (fabs(x) < EPS) x = T(0);
     if (fabs(y) < EPS) y = T(0);
     if (fabs(depth) < EPS) depth = T(0);
     if (x == T(0) && y == T(0) && depth == T(0)) return false;
-    ub0_disp<T>(x, y, depth, SD, CD, alp3, us, ud);
+    ub0_disp<T>(x, y, depth, SD, CD, aSD, aSC, us, ud);
+    return true;
+}
+// FP64: the same guards as integer tests on the bit patterns (the comparisons
+// would otherwise occupy the FP64 pipe): |v| < 1e-6 is |bits| < bits(1e-6)
+// for finite and NaN v alike, and depth < 0 is a set sign bit on a nonzero,
+// non-NaN value.
+template <>
+__device__ __forceinline__ bool dc3d0_disp<double>(double x, double y, double depth, double SD, double CD,
+                                                   double aSD, double aSC, double us[3], double ud[3]) {
+    const unsigned long long MAG = 0x7FFFFFFFFFFFFFFFull, INF = 0x7FF0000000000000ull;
+    const unsigned long long EPSB = 0x3EB0C6F7A0B5ED8Dull;   // 1.0e-6
+    const unsigned long long bx = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long by = (unsigned long long)__double_as_longlong(y);
+    const unsigned long long bd = (unsigned long long)__double_as_longlong(depth);
+    if ((bd >> 63) && (bd & MAG) != 0 && (bd & MAG) <= INF) return false;
+    const bool zx = (bx & MAG) < EPSB, zy = (by & MAG) < EPSB, zd = (bd & MAG) < EPSB;
+    if (zx && zy && zd) return false;
+    ub0_disp<double>(zx ? 0.0 : x, zy ? 0.0 : y, zd ? 0.0 : depth, SD, CD, aSD, aSC, us, ud);
     return true;
 }
 
@@ -197,10 +219,20 @@ __global__ void __launch_bounds__(128) greens_kernel(MeshDev m, int n_theta, con
         T dxi = (T)pg.dxi, deta = (T)pg.deta;
         T lxi2 = (T)(pg.lxi / 2.0), leta2 = (T)(pg.leta / 2.0);
         T area = dxi * deta;
+        const T aSD = alp3 * SD, aSC = alp3 * SD * CD;
+        T wa[MAXQ];   // area * w_a / 4 (the quadrature weight w_b completes it)
+        for (int a = 0; a < nq; ++a) wa[a] = area * qw[a] * T(0.25);
         if (BASIS == 0)
             for (int q = 0; q < (nxi + 1) * 6; ++q) pend[q] = T(0);
         for (int j = 0; j < neta; ++j) {
             T eta0 = (T)j * deta - leta2;
+            // receiver offsets along dip for this patch row's Gauss points
+            T yb[MAXQ], db[MAXQ];
+            for (int b = 0; b < nq; ++b) {
+                const T eta = eta0 + qx[b] * deta;
+                yb[b] = ys - eta * cdip;
+                db[b] = -(zf + eta * sdip);
+            }
             T carry_b[6], carry_t[6];
             for (int q = 0; q < 6; ++q) { carry_b[q] = T(0); carry_t[q] = T(0); }
             for (int i = 0; i < nxi; ++i) {
@@ -213,12 +245,9 @@ __global__ void __launch_bounds__(128) greens_kernel(MeshDev m, int n_theta, con
                     T xi = xi0 + qx[a] * dxi;
                     T x = xs - xi;
                     for (int b = 0; b < nq; ++b) {
-                        T eta = eta0 + qx[b] * deta;
-                        T y = ys - eta * cdip;
-                        T dep = -(zf + eta * sdip);
                         T us[3], ud[3];
-                        if (!dc3d0_disp<T>(x, y, dep, SD, CD, alp3, us, ud)) continue;
-                        T w = area * qw[a] * qw[b] * T(0.25);
+                        if (!dc3d0_disp<T>(x, yb[b], db[b], SD, CD, aSD, aSC, us, ud)) continue;
+                        T w = wa[a] * qw[b];
                         if (BASIS == 0) {
                             T r1 = (T)m.gq_x[a], r2 = (T)m.gq_x[b];
                             T nv[4] = {(T(1) - r1) * (T(1) - r2) * T(0.25), (T(1) + r1) * (T(1) - r2) * T(0.25),
