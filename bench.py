@@ -206,8 +206,8 @@ def nested_bench(pkg, torch, stages=1, cpu=True):
         out[name] = {"outer_particles_per_s": w.n_outer / per_stage, "s_per_outer_stage": per_stage,
                      "nested_evals_per_s": 2 * w.n_outer / per_stage, "init_eval_s": times[-1]}
     # evidence agreement on the true geometry over independent streams
-    # (256 per precision: standard error about 0.06 nat)
-    reps = 256
+    # (1024 per precision: standard error about 0.03 nat)
+    reps = 1024
     thr = np.repeat(th_true[None], reps, 0)
     st = np.arange(reps, dtype=np.uint64)
     res = {}

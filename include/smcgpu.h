@@ -99,9 +99,10 @@ typedef struct smcgpu_config {
                                       particle, 1, 2, 4 or 8; 0 picks from the batch size.
                                       Results do not depend on it.                      */
     int32_t inner_engine;          /* MIXED leapfrog engine, SMCGPU_ENGINE_*: warp-level
-                                      tensor-core MMA (default), CUDA cores, or tcgen05;
-                                      the tensor-core engines take slip dimensions <= 128
-                                      and fall back to CUDA cores above                 */
+                                      tensor-core MMA (default; slip dimensions <= 256,
+                                      the stage matrix streamed from global memory above
+                                      128), CUDA cores (<= 192), or tcgen05 (<= 128, CUDA
+                                      cores above).  FP64 takes slip dimensions <= 128.  */
 } smcgpu_config;
 
 typedef struct smcgpu_ctx smcgpu_ctx;

@@ -35,12 +35,21 @@ int next_pow2(int n) {
     return p;
 }
 
+// streamed stage matrix of the warp-MMA inner engine: uint4 per geometry (0 when unused)
+size_t afrag_per_theta(const smcgpu_ctx *ctx) {
+    const int D = ctx->mesh.D;
+    const bool streamed = ctx->cfg.precision == SMCGPU_PREC_MIXED && ctx->cfg.inner_engine == SMCGPU_ENGINE_MMA &&
+                          D > 128 && D <= 256;
+    return streamed ? (size_t)256 * 256 / 4 : 0;
+}
+
 size_t bytes_per_theta(const smcgpu_ctx *ctx) {
     const smc::MeshPattern &p = ctx->mesh;
     size_t D = p.D, N = ctx->cfg.nparticle_slip, NP2 = next_pow2((int)N);
     size_t b = D * ctx->nobs * 8 + D * std::max(ctx->nsar, 0) * 8 + D * D * 12 + D * 8 + 8;
     b += (size_t)p.nrow * 9 * 8 + D * 9 * 8 + p.ll_col.size() * 8 + sizeof(smc::ThetaAux);
     b += 2 * N * D * 8 + 9 * N * 8 + 4 * NP2 * 4 + p.nplane * sizeof(smc::PlaneGeom) + 64;
+    b += afrag_per_theta(ctx) * sizeof(uint4);
     return b;
 }
 
@@ -72,6 +81,7 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
     CU(ctx->d_A32.ensure((size_t)chunk * D * D), "alloc A32");
     CU(ctx->d_lv32.ensure((size_t)chunk * std::max(pm.nrow, 1) * 9), "alloc lv32");
     CU(ctx->d_ll32.ensure((size_t)chunk * std::max<size_t>(pm.ll_col.size(), 1)), "alloc ll32");
+    if (afrag_per_theta(ctx)) CU(ctx->d_afrag.ensure((size_t)chunk * afrag_per_theta(ctx)), "alloc stage matrices");
     CU(ctx->d_nstage_tmp.ensure((size_t)chunk), "alloc");
     for (int t0 = 0; t0 < n; t0 += chunk) {
         int nb = std::min(chunk, n - t0);
@@ -102,6 +112,7 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
         a.A32 = ctx->d_A32.p;
         a.lv32 = ctx->d_lv32.p;
         a.ll32 = ctx->d_ll32.p;
+        a.afrag = afrag_per_theta(ctx) ? ctx->d_afrag.p : nullptr;
         a.warps_per_theta = ctx->cfg.inner_warps;
         a.engine = ctx->cfg.inner_engine;
         cudaError_t e = smc::launch_inner(ctx->md, a, s, &why);

@@ -76,6 +76,14 @@ __device__ __forceinline__ void mma16816(float d[4], const uint32_t a[4], const 
 }
 __device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t *>(&v); }
 
+// ---- 16-byte asynchronous global -> shared copies (L2 only), in commit groups
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int NPEND>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(NPEND) : "memory"); }
+
 __device__ __forceinline__ double wsum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
@@ -338,17 +346,32 @@ __device__ __forceinline__ void warp_gemm(const T *__restrict__ Mcol, const T *_
 template <typename T, int RT, int ENG>
 struct Layout {
     static constexpr int DP = RGW * RT;
-    static constexpr int S = ENG == ENG_CC ? CW : 2048 / DP;   // slots per warp (CC) / per group
+    // warp-MMA engine beyond 128 dimensions: the stage matrix (4 DP^2 bytes as
+    // BF16 hi + lo) no longer fits in shared memory; it is kept in global memory
+    // in fragment order and streamed through a per-warp ring, and the FP32 Gram
+    // matrix of the end-point energies is read from global memory
+    static constexpr bool AGL = ENG == ENG_MMA && DP > 128;
+    static constexpr int S = ENG == ENG_CC ? CW : (AGL ? 4096 / DP : 2048 / DP);   // slots per warp (CC) / group
+    static constexpr int RING = 4;                       // streamed k-tiles in flight per warp
     static constexpr uint32_t LBO_A = 2048;              // tcgen05: 128 rows x 16 B per k block
     static constexpr uint32_t LBO_B = 16 * S + 16;       // tcgen05: S rows x 16 B per k block, padded
-    static constexpr size_t A_BYTES = ENG == ENG_TC ? (size_t)LBO_A * (DP / 8) : (size_t)DP * (DP + 8) * 2;
+    static constexpr size_t A_BYTES = ENG == ENG_TC ? (size_t)LBO_A * (DP / 8) : AGL ? 0 : (size_t)DP * (DP + 8) * 2;
     static constexpr size_t B_BYTES = ENG == ENG_TC ? (size_t)LBO_B * (DP / 8) : (size_t)DP * (S + 8) * 2;
     static constexpr int AST = DP + 8, BST = S + 8, TS = S + 1;   // warp-MMA row strides (elements)
     static constexpr size_t TILE_BYTES = (size_t)DP * TS * sizeof(float);
+    // m-tiles per warp of the warp-MMA step with W warps
+    __host__ __device__ static constexpr int mtiles_per_warp(int W) {
+        return (DP / 16) * (S / 8) / W > S / 8 ? (DP / 16) / W : 1;
+    }
+    // streamed A ring: RING slots x m-tiles x (hi, lo) x 32 lanes x 16 bytes per warp
+    __host__ __device__ static size_t ring_bytes(int W) {
+        return AGL ? (size_t)W * RING * mtiles_per_warp(W) * 2 * 32 * 16 : 0;
+    }
     __host__ __device__ static size_t engine_bytes(int W) {
         if (ENG == ENG_TC) return 2 * A_BYTES + 2 * B_BYTES;   // the end-point tile Xf aliases B
-        if (ENG == ENG_MMA)   // + the FP32 Gram matrix for the end-point energies
-            return 2 * A_BYTES + 4 * B_BYTES + 3 * TILE_BYTES + (size_t)DP * DP * sizeof(float);
+        if (ENG == ENG_MMA)   // + the FP32 Gram matrix for the end-point energies (or the A ring)
+            return 2 * A_BYTES + 4 * B_BYTES + 3 * TILE_BYTES +
+                   (AGL ? ring_bytes(W) : (size_t)DP * DP * sizeof(float));
         return (size_t)DP * DP * sizeof(T) + (size_t)W * 2 * DP * CW * sizeof(T);
     }
     __host__ __device__ static int slots(int W) { return ENG == ENG_CC ? W * CW : S; }
@@ -380,13 +403,15 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
     T *Msm = nullptr, *Xw0 = nullptr, *Xw1 = nullptr;
     unsigned char *Ahi = nullptr, *Alo = nullptr, *Bhi = nullptr, *Blo = nullptr;
     float *Xf = nullptr, *tX = nullptr, *tP = nullptr, *tXC = nullptr, *tA32 = nullptr;
+    uint4 *aring = nullptr;
     if constexpr (ENG == ENG_MMA) {
         // B buffer b: hi at Bhi + 2*b*B_BYTES, lo B_BYTES after it
         Ahi = sp; Alo = Ahi + L_::A_BYTES; Bhi = Alo + L_::A_BYTES; Blo = Bhi + L_::B_BYTES;
         tX = (float *)(Bhi + 4 * L_::B_BYTES);
         tP = (float *)((unsigned char *)tX + L_::TILE_BYTES);
         tXC = (float *)((unsigned char *)tP + L_::TILE_BYTES);
-        tA32 = (float *)((unsigned char *)tXC + L_::TILE_BYTES);
+        if constexpr (L_::AGL) aring = (uint4 *)((unsigned char *)tXC + L_::TILE_BYTES);
+        else tA32 = (float *)((unsigned char *)tXC + L_::TILE_BYTES);
         static_assert(2 * L_::B_BYTES >= L_::TILE_BYTES, "offset tile must fit in one B buffer");
     } else if constexpr (TC) {
         Ahi = sp; Alo = Ahi + L_::A_BYTES; Bhi = Alo + L_::A_BYTES; Blo = Bhi + L_::B_BYTES;
@@ -447,9 +472,13 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
     float *ll32 = a.ll32 ? a.ll32 + (size_t)th * m.ll_nnz : nullptr;
     float *wf = (float *)(Lc + 8 * N);   // MIXED: FP32 copy of the normalised weights
     if constexpr (ENG == ENG_MMA) {
-        for (int e = gt; e < DP * DP; e += gnt) {
-            const int k = e / DP, r = e % DP;
-            tA32[e] = (k < D && r < D) ? (float)Ath[(size_t)k * D + r] : 0.0f;
+        if constexpr (L_::AGL) {
+            for (int e = gt; e < D * D; e += gnt) A32[e] = (float)Ath[e];
+        } else {
+            for (int e = gt; e < DP * DP; e += gnt) {
+                const int k = e / DP, r = e % DP;
+                tA32[e] = (k < D && r < D) ? (float)Ath[(size_t)k * D + r] : 0.0f;
+            }
         }
         for (int e = gt; e < m.nrow * 9; e += gnt) lv32[e] = (float)lv[e];
         for (int e = gt; e < m.ll_nnz; e += gnt) ll32[e] = (float)llv[e];
@@ -653,7 +682,42 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
             }
         }
         // ---- stage matrix
-        if constexpr (ENG == ENG_MMA) {
+        if constexpr (L_::AGL) {
+            // M = gamma A + L^T L / alpha^2 in FP32 from the global FP32 copy of A,
+            // split into BF16 hi + lo and stored in m16n8k16 A-fragment order:
+            // [m-tile][k-tile][hi, lo][lane] x 16 bytes, register j of lane (g, t4)
+            // holding row 16 mt + g + 8 (j & 1), columns 16 kt + 2 t4 + 8 (j >> 1) + {0, 1}
+            constexpr int KT = DP / 16;
+            const float gf = (float)gamma, ia2 = (float)(1.0 / alpha2);
+            uint4 *fr = a.afrag + (size_t)th * (DP * DP / 4);
+            for (int q = gt; q < KT * KT * 32; q += gnt) {
+                const int ln = q & 31, tile = q >> 5, mt = tile / KT, kt = tile % KT;
+                const int g8 = ln >> 2, t4 = ln & 3;
+                uint32_t hw[4], lw[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int i = 16 * mt + g8 + 8 * (j & 1), k0 = 16 * kt + 2 * t4 + 8 * (j >> 1);
+                    float v[2];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int k = k0 + h;
+                        float vv = 0.0f;
+                        if (i < D && k < D) {
+                            vv = gf * A32[(size_t)k * D + i];
+                            for (int e = m.ll_ptr[i]; e < m.ll_ptr[i + 1]; ++e)
+                                if (m.ll_col[e] == k) { vv += ll32[e] * ia2; break; }
+                        }
+                        v[h] = vv;
+                    }
+                    const __nv_bfloat162 hi = __floats2bfloat162_rn(v[0], v[1]);
+                    const __nv_bfloat162 lo = __floats2bfloat162_rn(v[0] - __low2float(hi), v[1] - __high2float(hi));
+                    hw[j] = bf16x2_bits(hi);
+                    lw[j] = bf16x2_bits(lo);
+                }
+                fr[(size_t)(2 * tile) * 32 + ln] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                fr[(size_t)(2 * tile + 1) * 32 + ln] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+        } else if constexpr (ENG == ENG_MMA) {
             // M = gamma A + L^T L / alpha^2 in FP32 (A from the FP32 copy in shared
             // memory), split into BF16 hi + lo, row-major with row stride DP+8;
             // TPR threads per row, KC consecutive columns each
@@ -835,6 +899,24 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
 #pragma unroll
                     for (int kt = 0; kt < KT; ++kt) load_a(kt, kt);
                 }
+                // streamed A (beyond 128 dimensions): k-tile kt of this warp's m-tiles
+                // goes to ring slot kt % RING; every lane copies and later reads only
+                // its own 16-byte fragments, so no warp barrier is needed
+                constexpr int RING = L_::RING;
+                const uint4 *afr = L_::AGL ? a.afrag + (size_t)th * (DP * DP / 4) : nullptr;
+                uint4 *wring = L_::AGL ? aring + (size_t)wl * RING * MTW * 64 : nullptr;
+                auto issue_a = [&](int kt) {
+                    if (kt < KT) {
+#pragma unroll
+                        for (int aa = 0; aa < MTW; ++aa) {
+                            const uint4 *src = afr + (size_t)(2 * ((mt0 + aa) * KT + kt)) * 32 + lane;
+                            uint4 *dst = wring + (size_t)(2 * ((kt % RING) * MTW + aa)) * 32 + lane;
+                            cp_async16(dst, src);
+                            cp_async16(dst + 32, src + 32);
+                        }
+                    }
+                    cp_async_commit();   // an empty group past the last k-tile keeps the count uniform
+                };
                 // offsets from the stage mean of the lane's entries -> BF16 hi/lo operand buffer
                 auto write_b = [&](int buf) {
                     __nv_bfloat16 *bh = (__nv_bfloat16 *)(Bhi + 2 * (size_t)buf * L_::B_BYTES);
@@ -961,6 +1043,10 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
 #pragma unroll
                                 for (int e = 0; e < 4; ++e) acc[aa][bb][e] = acc1[aa][bb][e] = acc2[aa][bb][e] = 0.0f;
                         constexpr int KTB = (NTW * KT <= 8) ? KT : 1;   // k-tiles of B fragments held at once
+                        if constexpr (L_::AGL) {
+#pragma unroll
+                            for (int kt = 0; kt < RING - 1; ++kt) issue_a(kt);
+                        }
 #pragma unroll
                         for (int k0 = 0; k0 < KT; k0 += KTB) {
                             uint32_t fbh[KTB][NTW][2], fbl[KTB][NTW][2];
@@ -976,7 +1062,19 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
 #pragma unroll
                             for (int kk = 0; kk < KTB; ++kk) {
                                 const int kt = k0 + kk;
-                                if constexpr (!AREG) load_a(kt, 0);
+                                if constexpr (L_::AGL) {
+                                    // groups committed so far: k-tiles 0 .. kt + RING - 1;
+                                    // at most RING - 1 pending means k-tile kt has landed
+                                    issue_a(kt + RING - 1);
+                                    cp_async_wait<RING - 1>();
+#pragma unroll
+                                    for (int aa = 0; aa < MTW; ++aa) {
+                                        const uint4 *rs = wring + (size_t)(2 * ((kt % RING) * MTW + aa)) * 32 + lane;
+                                        const uint4 h = rs[0], l = rs[32];
+                                        fah[aa][0][0] = h.x; fah[aa][0][1] = h.y; fah[aa][0][2] = h.z; fah[aa][0][3] = h.w;
+                                        fal[aa][0][0] = l.x; fal[aa][0][1] = l.y; fal[aa][0][2] = l.z; fal[aa][0][3] = l.w;
+                                    }
+                                } else if constexpr (!AREG) load_a(kt, 0);
                                 const int ks = AREG ? kt : 0;
 #pragma unroll
                                 for (int aa = 0; aa < MTW; ++aa)
@@ -1069,9 +1167,16 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                         for (int i = 0; i < RPT; ++i) af[i] = 0.0f;
                         for (int k = 0; k < D; ++k) {
                             const float dk = dl[k * TS + cs];
-                            const float *ak = tA32 + k * DP + part;
+                            if constexpr (L_::AGL) {
+                                const float *ak = A32 + (size_t)k * D + part;
 #pragma unroll
-                            for (int i = 0; i < RPT; ++i) af[i] = fmaf(ak[i * NPART], dk, af[i]);
+                                for (int i = 0; i < RPT; ++i)
+                                    if (part + i * NPART < D) af[i] = fmaf(ak[i * NPART], dk, af[i]);
+                            } else {
+                                const float *ak = tA32 + k * DP + part;
+#pragma unroll
+                                for (int i = 0; i < RPT; ++i) af[i] = fmaf(ak[i * NPART], dk, af[i]);
+                            }
                         }
 #pragma unroll
                         for (int i = 0; i < RPT; ++i) {
@@ -1787,6 +1892,12 @@ cudaError_t launch_inner(const MeshDev &m, const InnerArgs &a, cudaStream_t s, c
         if (D <= 64) return launch_cc_t<double, 4>(m, a, s, W);
         if (D <= 96) return launch_cc_t<double, 6>(m, a, s, W);
         if (D <= 128) return launch_cc_t<double, 8>(m, a, s, W);
+        *why = "slip dimension too large for the FP64 inner kernel (D <= 128)";
+        return cudaErrorInvalidValue;
+    } else if (a.engine == SMCGPU_ENGINE_MMA && D > 128 && D <= 256) {
+        // stage matrix streamed from global memory, one geometry per CTA of 16 warps
+        if (!a.afrag || !a.A32) { *why = "inner kernel: stage-matrix buffers missing"; return cudaErrorInvalidValue; }
+        return launch_wg_t<16, ENG_MMA, 16>(m, a, s, 1);
     } else if (a.engine == SMCGPU_ENGINE_MMA && D <= 128) {
         // 16 warps per geometry while the batch leaves SMs free (lowest
         // latency per geometry), 8 warps and two geometries per CTA beyond
@@ -1808,7 +1919,8 @@ cudaError_t launch_inner(const MeshDev &m, const InnerArgs &a, cudaStream_t s, c
         if (D <= 128) return launch_cc_t<float, 8>(m, a, s, W);
         if (D <= 192) return launch_cc_t<float, 12>(m, a, s, W);
     }
-    *why = "slip dimension too large for the shared-memory inner kernel";
+    *why = "slip dimension too large for the MIXED inner kernel (warp MMA: D <= 256, CUDA cores: D <= 192, "
+           "tcgen05: D <= 128)";
     return cudaErrorInvalidValue;
 }
 

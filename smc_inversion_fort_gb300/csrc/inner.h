@@ -13,7 +13,7 @@ struct InnerArgs {
     int n_theta, N, NP2, D, mixed;
     int ntau, tf, max_stages;
     int warps_per_theta;  // CUDA-core engine: warps per geometry (1, 2, 4, 8; 0 picks by batch size)
-    int engine;           // MIXED step engine, SMCGPU_ENGINE_* (tensor-core engines need D <= 128)
+    int engine;           // MIXED step engine, SMCGPU_ENGINE_* (warp MMA: D <= 256, tcgen05: D <= 128)
     double cv, max_slip;
     uint64_t seed;
     const unsigned long long *streams;  // [n_theta]
@@ -22,6 +22,7 @@ struct InnerArgs {
     float *A32;           // [th][D][D] FP32 copy (MIXED), written by the inner kernel
     float *lv32;          // [th][nrow][9] FP32 copy of the L values (MIXED), written by the inner kernel
     float *ll32;          // [th][ll_nnz] FP32 copy of the L^T L values (MIXED), written by the inner kernel
+    uint4 *afrag;         // [th][256 * 256 / 4] stage matrix in MMA-fragment order (MIXED, 128 < D <= 256)
     const double *b;      // [th][D]
     const double *dsd;    // [th]
     const double *lval;   // [th][nrow][9] values of L (columns in MeshDev::l_col)

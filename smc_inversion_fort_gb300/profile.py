@@ -24,6 +24,7 @@ def main(argv=None):
     p.add_argument("--reps", type=int, default=2)
     p.add_argument("--warps", type=int, default=0, help="inner kernel warps per geometry (0: by batch size)")
     p.add_argument("--engine", choices=["mma", "cuda", "tcgen05"], default="mma", help="MIXED inner step engine")
+    p.add_argument("--workload", default="c0", help="nested: named workload (c0, c2, d160, d256, ...)")
     a = p.parse_args(argv)
     import torch
 
@@ -48,7 +49,7 @@ def main(argv=None):
             torch.cuda.synchronize()
             print(f"greens n_theta={n} {'fp32' if a.fp32 else 'fp64'}: {1e3 * (time.perf_counter() - t0):.2f} ms")
     else:
-        w = preset("c0")
+        w = preset(a.workload)
         w.settings.inner_warps = a.warps
         w.settings.inner_engine = {"mma": 0, "cuda": 1, "tcgen05": 2}[a.engine]
         n = a.n_theta or 16
@@ -65,7 +66,8 @@ def main(argv=None):
         for r in range(a.reps):
             t0 = time.perf_counter()
             nl, st = g.fault_calc_likelihood(th, 1, np.arange(n, dtype=np.uint64) + 1000 * r)
-            print(f"nested n_theta={n} warps={a.warps} {a.engine} {'mixed' if a.mixed else 'fp64'}: {time.perf_counter() - t0:.3f} s, "
+            print(f"nested {a.workload} n_theta={n} warps={a.warps} {a.engine} {'mixed' if a.mixed else 'fp64'}: "
+                  f"{time.perf_counter() - t0:.3f} s, "
                   f"-logZ[0] {nl[0]:.4f}, status {int(st.max())}")
 
 
