@@ -41,6 +41,7 @@ def parse():
     p.add_argument("--n-theta", type=int, default=8192)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-nested", action="store_true")
+    p.add_argument("--no-c2", action="store_true", help="skip the c2 (D = 256) nested sample")
     p.add_argument("--outer-stages", type=int, default=1)
     return p.parse_args()
 
@@ -227,6 +228,38 @@ def nested_bench(pkg, torch, stages=1, cpu=True):
     return out
 
 
+def nested_c2_bench(pkg, torch):
+    """Nested evaluations/s on c2 (16x8 patches x 2 components, D = 256; 400
+    GNSS stations and 2000 InSAR points in two paths with a 5 km exponential
+    covariance, 3200 observations; 2048 inner particles, ntau 50), MIXED.
+    Sample: one wave of prior geometries, one per SM (the inner kernel runs one
+    geometry per CTA at this size), after a small warm-up batch."""
+    from smc_inversion_fort_gb300.configs import make_stations, preset, random_thetas, true_slip, true_theta
+    w = preset("c2")
+    rng = np.random.default_rng(2024)
+    obs = make_stations(w, rng)
+    obs["dvec"] = np.zeros(len(obs["obs_sigma"]))
+    g = pkg.SmcGpu(w.settings, pkg.PREC_MIXED)
+    g.set_data(obs)
+    G = g.calc_greens_func(true_theta(w)[None])[0]
+    obs["dvec"] = G.T @ true_slip(w) + rng.standard_normal(G.shape[1]) * obs["obs_sigma"]
+    g.set_data(obs)
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    g.fault_calc_likelihood(random_thetas(w, 8, seed=11), 5, np.arange(8, dtype=np.uint64))
+    th = random_thetas(w, nsm, seed=12)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nl, st = g.fault_calc_likelihood(th, 6, np.arange(nsm, dtype=np.uint64) + 100)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    g.close()
+    return {"workload": "c2: 16x8 patches (D=256), 400 GNSS + 2000 InSAR points (3200 obs, 5 km exponential "
+                        "covariance), 2048 inner particles, ntau 50, MIXED",
+            "sample": f"{nsm} prior geometries in one batch (one wave, one geometry per SM)",
+            "nested_evals_per_s": nsm / dt, "outer_particles_per_s": nsm / dt / 2, "s_per_batch": dt,
+            "status_max": int(st.max()), "neglog_median": float(np.median(nl))}
+
+
 def cpu_nested_rate(w, obs, rg, target_s=15.0):
     """Oracle nested evaluations of prior-box geometries on all host threads
     (one geometry per thread, as the reference's MPI ranks); outer particles
@@ -384,6 +417,8 @@ def gb300_arm(args):
         torch.cuda.empty_cache()
         line["nested_smc"] = nested_bench(pkg, torch, stages=args.outer_stages,
                                           cpu=(rank == 0 and not args.no_cpu_baseline))
+        if not args.no_c2:
+            line["nested_smc_c2"] = nested_c2_bench(pkg, torch)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -12,6 +12,7 @@
  * Reference interfaces replaced (paths inside KaiNakao/smc_inversion_fort):
  *   smcgpu_set_data            main.f90:254-307 + init.f90:5-119 (data, Sigma_SAR^-1)
  *   smcgpu_greens_batch        gfunc.f90:242-348 calc_greens_func, batched over theta
+ *   smcgpu_gram_batch          smc_slip.f90:1347-1443 slip_calc_gsd_gsg, batched over theta
  *   smcgpu_fault_likelihood_batch
  *                              smc_fault.f90:66-292 fault_calc_likelihood, batched
  *                              (discretize_fault, gen_laplacian, calc_greens_func,
@@ -143,6 +144,14 @@ int32_t smcgpu_greens_batch(smcgpu_ctx *ctx, int32_t n_theta, const double *thet
                             void *gmat);
 int32_t smcgpu_greens_batch_dev(smcgpu_ctx *ctx, int32_t n_theta, const double *theta_dev,
                                 int32_t precision, void *gmat_dev);
+
+/* slip_calc_gsd_gsg (smc_slip.f90:1347-1443) for n_theta geometries, FP64:
+ * gsgmat(D, D, n_theta) = G^T Sigma^-1 G, gsdvec(D, n_theta) = G^T Sigma^-1 d and
+ * dsd(n_theta) = d^T Sigma^-1 d, with each theta's hyperparameters scaling the
+ * InSAR and GNSS blocks (sigma2_sar, sigma2_gnss).  The InSAR blocks go through
+ * the whitening factor of Sigma_SAR^-1 made in set_data.  Host buffers. */
+int32_t smcgpu_gram_batch(smcgpu_ctx *ctx, int32_t n_theta, const double *theta, double *gsgmat,
+                          double *gsdvec, double *dsd);
 
 /* smcgpu_greens_batch_dev for callers that cannot allocate device memory
  * during the call: hosts that give the whole GPU memory to their own pool

@@ -80,6 +80,7 @@ def load_library() -> C.CDLL:
         "smcgpu_dims": (i32, [vp, P(i32), P(i32), P(i32), P(i32)]),
         "smcgpu_greens_batch": (i32, [vp, i32, vp, i32, vp]),
         "smcgpu_greens_batch_dev": (i32, [vp, i32, vp, i32, vp]),
+        "smcgpu_gram_batch": (i32, [vp, i32, vp, vp, vp, vp]),
         "smcgpu_fault_likelihood_batch": (i32, [vp, i32, vp, u64, vp, vp, vp]),
         "smcgpu_fault_likelihood_batch_dev": (i32, [vp, i32, vp, u64, vp, vp, vp]),
         "smcgpu_fault_likelihood_trace": (i32, [vp, i32, vp, u64, vp, vp, vp, vp, vp, vp]),
@@ -113,7 +114,8 @@ def load_library() -> C.CDLL:
 
 EXPORTED_SYMBOLS = [
     "smcgpu_default_config", "smcgpu_create", "smcgpu_destroy", "smcgpu_set_data", "smcgpu_set_stream",
-    "smcgpu_dims", "smcgpu_greens_batch", "smcgpu_greens_batch_dev", "smcgpu_fault_likelihood_batch",
+    "smcgpu_dims", "smcgpu_greens_batch", "smcgpu_greens_batch_dev", "smcgpu_gram_batch",
+    "smcgpu_fault_likelihood_batch",
     "smcgpu_fault_likelihood_batch_dev", "smcgpu_fault_likelihood_trace", "smcgpu_fault_likelihood_posterior",
     "smcgpu_fault_smc_exec", "smcgpu_fault_smc_exec_gsmc", "smcgpu_fault_smc_resume", "smcgpu_resample_counts",
     "smcgpu_qsort_",
@@ -218,6 +220,16 @@ class SmcGpu:
 
     def greens_dev(self, n_theta: int, theta_ptr: int, gmat_ptr: int, precision: int = PREC_FP64):
         self._check(self.lib.smcgpu_greens_batch_dev(self.h, n_theta, theta_ptr, precision, gmat_ptr), "greens_batch_dev")
+
+    def gram(self, theta: np.ndarray):
+        """slip_calc_gsd_gsg (smc_slip.f90:1347-1443) per theta: (gsgmat [n, D, D]
+        with gsgmat[t, j, i] = A(i, j), gsdvec [n, D], dsd [n])."""
+        th = np.ascontiguousarray(np.atleast_2d(theta), dtype=np.float64)
+        D = self.dims()["D"]
+        n = th.shape[0]
+        A, b, dsd = np.empty((n, D, D)), np.empty((n, D)), np.empty(n)
+        self._check(self.lib.smcgpu_gram_batch(self.h, n, _ptr(th), _ptr(A), _ptr(b), _ptr(dsd)), "gram_batch")
+        return A, b, dsd
 
     # fault_calc_likelihood, batched (smc_fault.f90:66-292)
     def fault_calc_likelihood(self, theta: np.ndarray, seed: int, streams=None):

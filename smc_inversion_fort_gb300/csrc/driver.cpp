@@ -134,6 +134,44 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
     return SMCGPU_OK;
 }
 
+// G, then the Gram products, for n thetas already on the device, in chunks;
+// the products are copied to the host buffers after each chunk
+int gram_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, double *gsg, double *gsd, double *dsd) {
+    const smc::MeshPattern &pm = ctx->mesh;
+    const int D = pm.D, nd = pm.ndim_fault;
+    cudaStream_t s = ctx->stream;
+    const size_t per = (size_t)D * ctx->nobs * 8 + (size_t)D * std::max(ctx->nsar, 0) * 8 + (size_t)D * D * 8 +
+                       (size_t)D * 8 + (size_t)pm.nrow * 9 * 8 + (size_t)D * 9 * 8 + pm.ll_col.size() * 8 + 256;
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)n, ((size_t)4 << 30) / per));
+    CU(ctx->d_planes.ensure((size_t)chunk * pm.nplane), "alloc");
+    CU(ctx->d_gmat.ensure((size_t)chunk * D * ctx->nobs), "alloc gmat");
+    CU(ctx->d_gw.ensure((size_t)chunk * D * std::max(ctx->nsar, 1)), "alloc gw");
+    CU(ctx->d_A.ensure((size_t)chunk * D * D), "alloc A");
+    CU(ctx->d_b.ensure((size_t)chunk * D), "alloc b");
+    CU(ctx->d_dsd.ensure((size_t)chunk), "alloc dsd");
+    CU(ctx->d_lval.ensure((size_t)chunk * pm.nrow * 9), "alloc lval");
+    CU(ctx->d_ltval.ensure((size_t)chunk * D * 9), "alloc ltval");
+    CU(ctx->d_llval.ensure((size_t)chunk * std::max<size_t>(pm.ll_col.size(), 1)), "alloc llval");
+    CU(ctx->d_aux.ensure((size_t)chunk), "alloc aux");
+    for (int t0 = 0; t0 < n; t0 += chunk) {
+        const int nb = std::min(chunk, n - t0);
+        const double *th = theta_dev + (size_t)t0 * nd;
+        CU(smc::launch_planes(ctx->md, nb, th, ctx->d_planes.p, s), "planes kernel");
+        CU(smc::launch_greens(ctx->md, nb, ctx->d_planes.p, SMCGPU_PREC_FP64, ctx->d_gmat.p, s), "greens kernel");
+        CU(smc::launch_setup(ctx->md, nb, th, ctx->d_planes.p, ctx->d_lval.p, ctx->d_ltval.p, ctx->d_llval.p,
+                             ctx->d_aux.p, s), "setup kernel");
+        CU(smc::launch_gram(ctx->md, nb, ctx->d_gmat.p, ctx->d_roww.p, ctx->d_dx.p, ctx->d_aux.p, ctx->dsd_sar,
+                            ctx->dsd_gnss, ctx->d_A.p, ctx->d_b.p, ctx->d_dsd.p, ctx->d_gw.p, s), "gram kernel");
+        CU(cudaMemcpyAsync(gsg + (size_t)t0 * D * D, ctx->d_A.p, (size_t)nb * D * D * sizeof(double),
+                           cudaMemcpyDeviceToHost, s), "copy gsgmat");
+        CU(cudaMemcpyAsync(gsd + (size_t)t0 * D, ctx->d_b.p, (size_t)nb * D * sizeof(double), cudaMemcpyDeviceToHost,
+                           s), "copy gsdvec");
+        CU(cudaMemcpyAsync(dsd + t0, ctx->d_dsd.p, (size_t)nb * sizeof(double), cudaMemcpyDeviceToHost, s), "copy dsd");
+        CU(cudaStreamSynchronize(s), "sync");
+    }
+    return SMCGPU_OK;
+}
+
 int check_ready(smcgpu_ctx *ctx) {
     if (!ctx->has_data) return ctx->fail(SMCGPU_ERR_NODATA, "set_data not called");
     if (ctx->cfg.precision != SMCGPU_PREC_FP64 && ctx->cfg.precision != SMCGPU_PREC_MIXED)
@@ -142,6 +180,18 @@ int check_ready(smcgpu_ctx *ctx) {
 }
 
 }  // namespace
+
+extern "C" int32_t smcgpu_gram_batch(smcgpu_ctx *ctx, int32_t n_theta, const double *theta, double *gsgmat,
+                                     double *gsdvec, double *dsd) {
+    if (!ctx) return SMCGPU_ERR_ARG;
+    if (!ctx->has_data) return ctx->fail(SMCGPU_ERR_NODATA, "gram: set_data not called");
+    if (n_theta < 0 || (n_theta > 0 && (!theta || !gsgmat || !gsdvec || !dsd)))
+        return ctx->fail(SMCGPU_ERR_ARG, "gram: bad arguments");
+    if (n_theta == 0) return SMCGPU_OK;
+    CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+    CU(ctx->d_theta.upload(theta, (size_t)n_theta * ctx->mesh.ndim_fault, ctx->stream), "upload theta");
+    return gram_batch(ctx, n_theta, ctx->d_theta.p, gsgmat, gsdvec, dsd);
+}
 
 extern "C" int32_t smcgpu_resample_counts(smcgpu_ctx *ctx, const double *weights, int32_t n, double u0_hi,
                                           double u0_lo, int32_t *counts) {

@@ -352,7 +352,7 @@ struct Layout {
     // matrix of the end-point energies is read from global memory
     static constexpr bool AGL = ENG == ENG_MMA && DP > 128;
     static constexpr int S = ENG == ENG_CC ? CW : (AGL ? 4096 / DP : 2048 / DP);   // slots per warp (CC) / group
-    static constexpr int RING = 4;                       // streamed k-tiles in flight per warp
+    static constexpr int RING = 6;                       // streamed k-tiles in flight per warp
     static constexpr uint32_t LBO_A = 2048;              // tcgen05: 128 rows x 16 B per k block
     static constexpr uint32_t LBO_B = 16 * S + 16;       // tcgen05: S rows x 16 B per k block, padded
     static constexpr size_t A_BYTES = ENG == ENG_TC ? (size_t)LBO_A * (DP / 8) : AGL ? 0 : (size_t)DP * (DP + 8) * 2;
@@ -364,7 +364,7 @@ struct Layout {
         return (DP / 16) * (S / 8) / W > S / 8 ? (DP / 16) / W : 1;
     }
     // streamed A ring: RING slots x m-tiles x (hi, lo) x 32 lanes x 16 bytes per warp
-    __host__ __device__ static size_t ring_bytes(int W) {
+    __host__ __device__ static constexpr size_t ring_bytes(int W) {
         return AGL ? (size_t)W * RING * mtiles_per_warp(W) * 2 * 32 * 16 : 0;
     }
     __host__ __device__ static size_t engine_bytes(int W) {
@@ -375,10 +375,15 @@ struct Layout {
         return (size_t)DP * DP * sizeof(T) + (size_t)W * 2 * DP * CW * sizeof(T);
     }
     __host__ __device__ static int slots(int W) { return ENG == ENG_CC ? W * CW : S; }
+    // per-slot partial sums of the end-point energies: 5 x 32 W floats (warp MMA)
+    // or 5 x 32 max(W, 4) doubles (tcgen05)
+    __host__ __device__ static size_t red_bytes(int W) {
+        return ENG == ENG_MMA ? (size_t)5 * 32 * W * sizeof(float) : (size_t)5 * 32 * (W > 4 ? W : 4) * sizeof(double);
+    }
     __host__ __device__ static size_t bytes(int W) {
         size_t b = engine_bytes(W) + (size_t)7 * DP * sizeof(T) + (size_t)6 * DP * sizeof(double) +
                    (size_t)slots(W) * (5 * sizeof(double) + 5 * sizeof(int)) + (size_t)(4 * W + 8) * sizeof(double);
-        if (ENG != ENG_CC) b += (size_t)5 * 32 * (W > 4 ? W : 4) * sizeof(double) + 64;   // reductions, masks, mbarrier
+        if (ENG != ENG_CC) b += red_bytes(W) + 64;   // reductions, masks, mbarrier
         return (b + 127) & ~(size_t)127;
     }
 };
@@ -440,8 +445,8 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
     unsigned long long *masks = nullptr;   // [0] fresh, [1] active, [2] blown, [3] accepted
     uint64_t *mbar = nullptr;
     if constexpr (ENG != ENG_CC) {
-        red = (double *)(gint + 8);   // [5][32 W] per-slot partial sums
-        masks = (unsigned long long *)(red + 5 * 32 * (W > 4 ? W : 4));
+        red = (double *)(gint + 8);   // per-slot partial sums
+        masks = (unsigned long long *)((unsigned char *)red + L_::red_bytes(W));
         mbar = (uint64_t *)(masks + 4);
     }
 
@@ -1159,25 +1164,42 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                     // FP32 per-thread partial sums: the expansion point (the stage
                     // mean) is FP32-exact, so these are offsets from L(sbar), P(sbar)
                     float q0 = 0.0f, q1 = 0.0f, q2 = 0.0f, q3 = 0.0f;
-                    if ((actm >> cs) & 1ull) {
-                        // rows part + i NPART of A times the offsets: RPT independent chains
-                        constexpr int RPT = DP / NPART;
-                        float af[RPT];
+                    const bool slot_on = (actm >> cs) & 1ull;
+                    // rows part + i NPART of A times the offsets: RPT independent chains
+                    constexpr int RPT = DP / NPART;
+                    float af[RPT];
 #pragma unroll
-                        for (int i = 0; i < RPT; ++i) af[i] = 0.0f;
+                    for (int i = 0; i < RPT; ++i) af[i] = 0.0f;
+                    if constexpr (L_::AGL) {
+                        // the FP32 Gram matrix from global memory, KC columns at a time
+                        // staged through the A ring (idle: no copy is in flight here)
+                        float *As = (float *)aring;
+                        constexpr int KC = (int)(L_::ring_bytes(WG) / (DP * sizeof(float)));
+                        for (int k0 = 0; k0 < D; k0 += KC) {
+                            const int kn = min(KC, D - k0);
+                            grp.sync();
+                            for (int e = gt; e < kn * DP; e += NTH) {
+                                const int kk = e / DP, r = e % DP;
+                                As[e] = r < D ? A32[(size_t)(k0 + kk) * D + r] : 0.0f;
+                            }
+                            grp.sync();
+                            if (slot_on)
+                                for (int kk = 0; kk < kn; ++kk) {
+                                    const float dk = dl[(k0 + kk) * TS + cs];
+                                    const float *ak = As + kk * DP + part;
+#pragma unroll
+                                    for (int i = 0; i < RPT; ++i) af[i] = fmaf(ak[i * NPART], dk, af[i]);
+                                }
+                        }
+                    } else if (slot_on) {
                         for (int k = 0; k < D; ++k) {
                             const float dk = dl[k * TS + cs];
-                            if constexpr (L_::AGL) {
-                                const float *ak = A32 + (size_t)k * D + part;
+                            const float *ak = tA32 + k * DP + part;
 #pragma unroll
-                                for (int i = 0; i < RPT; ++i)
-                                    if (part + i * NPART < D) af[i] = fmaf(ak[i * NPART], dk, af[i]);
-                            } else {
-                                const float *ak = tA32 + k * DP + part;
-#pragma unroll
-                                for (int i = 0; i < RPT; ++i) af[i] = fmaf(ak[i * NPART], dk, af[i]);
-                            }
+                            for (int i = 0; i < RPT; ++i) af[i] = fmaf(ak[i * NPART], dk, af[i]);
                         }
+                    }
+                    if (slot_on) {
 #pragma unroll
                         for (int i = 0; i < RPT; ++i) {
                             const int r = part + i * NPART;
