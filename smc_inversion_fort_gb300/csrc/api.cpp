@@ -67,6 +67,8 @@ static void refresh_md(smcgpu_ctx *ctx) {
     m.lt_row = ctx->d_lt_row.p; m.lt_k = ctx->d_lt_k.p; m.lt_plane = ctx->d_lt_plane.p;
     m.ll_ptr = ctx->d_ll_ptr.p; m.ll_col = ctx->d_ll_col.p;
     m.ll_nnz = (int)p.ll_col.size(); m.ll_maxrow = p.ll_maxrow;
+    m.gb_order = ctx->d_gb_order.p; m.gb_lvl_ptr = ctx->d_gb_lvl_ptr.p;
+    m.gb_nlevel = (int)p.gb_lvl_ptr.size() - 1;
     m.nobs = ctx->nobs; m.nsar = ctx->nsar; m.ngnss = ctx->ngnss; m.nstation = ctx->nstation; m.npath = ctx->npath;
     m.st_x = ctx->d_st_x.p; m.st_y = ctx->d_st_y.p; m.st_row = ctx->d_st_row.p; m.st_nrow = ctx->d_st_nrow.p;
     m.obs_e = ctx->d_obs_e.p; m.obs_sigma = ctx->d_obs_sigma.p; m.dvec = ctx->d_dvec.p;
@@ -118,6 +120,8 @@ extern "C" int32_t smcgpu_create(const smcgpu_config *cfg, smcgpu_ctx **out) {
     up(ctx->d_lt_plane.upload(p.lt_plane, s));
     up(ctx->d_ll_ptr.upload(p.ll_ptr, s));
     up(ctx->d_ll_col.upload(p.ll_col, s));
+    up(ctx->d_gb_order.upload(p.gb_order, s));
+    up(ctx->d_gb_lvl_ptr.upload(p.gb_lvl_ptr, s));
     up(cudaStreamSynchronize(s));
     if (ce != cudaSuccess) {
         g_create_err = std::string("cuda: ") + cudaGetErrorString(ce);

@@ -37,6 +37,7 @@ struct smcgpu_ctx {
 
     // pattern tables
     smc::DevBuf<int> d_dof_of_node, d_l_col, d_l_plane, d_lt_row, d_lt_plane, d_ll_ptr, d_ll_col;
+    smc::DevBuf<int> d_gb_order, d_gb_lvl_ptr;
     smc::DevBuf<signed char> d_l_k, d_lt_k;
     // observations
     smc::DevBuf<double> d_st_x, d_st_y, d_obs_e, d_obs_sigma, d_dvec, d_sar_w, d_dx, d_roww;

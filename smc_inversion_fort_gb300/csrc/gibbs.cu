@@ -7,21 +7,13 @@
 
 namespace smc {
 
-namespace {
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-}  // namespace
-
 // One warp per geometry runs the reference's single chained sweep (particle
-// k is one sweep after particle k-1, starting at 0).  FP64 uses the
-// reference's Newton inverse CDF; MIXED inverts in FP32 through
-// normcdff/normcdfinvf on the tail-appropriate side.
-template <bool MIXED>
+// k is one sweep after particle k-1, starting at 0).  The sweep goes level by
+// level (MeshDev::gb_order): the components of a level are not coupled, so
+// the lanes update them together and the result equals the sequential sweep.
+// Each lane follows the reference's arithmetic for its component (the
+// conditional mean summed over j != i in ascending j, no contractions) and its
+// Newton inverse CDF.
 __global__ void gibbs_kernel(MeshDev m, InnerArgs a) {
     extern __shared__ double gsh[];
     const int wpb = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -38,74 +30,40 @@ __global__ void gibbs_kernel(MeshDev m, InnerArgs a) {
     __syncwarp();
     const double pi = 3.141592653589793;
     for (int k = 0; k < N; ++k) {
-        for (int d = lane; d < D; d += 32)
-            vn[d] = MIXED ? (double)rng_normal_f(a.seed, stream, RNG_GIBBS, 0, k, d)
-                          : rng_normal(a.seed, stream, RNG_GIBBS, 0, k, d);
+        for (int d = lane; d < D; d += 32) vn[d] = rng_normal(a.seed, stream, RNG_GIBBS, 0, k, d);
         __syncwarp();
-        for (int i = 0; i < D; ++i) {
-            int e0 = m.ll_ptr[i], e1 = m.ll_ptr[i + 1];
-            // diagonal entry and the conditional mean
-            int e = e0 + lane;
-            int j = e < e1 ? m.ll_col[e] : -1;
-            double v = e < e1 ? ll[e] : 0.0;
-            double s2, mu;
-            if (!MIXED) {
-                double lii = (j == i) ? v : 0.0, term = 0.0;
-                lii = warp_sum(lii);
-                s2 = 1.0 / (lii / alpha2);
-                if (j >= 0 && j != i) term = v / alpha2 * cur[j] * s2;
-                mu = -warp_sum(term);
-            } else {
-                float lii = (j == i) ? (float)v : 0.0f, term = 0.0f;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) lii += __shfl_xor_sync(0xffffffffu, lii, o);
-                if (j >= 0 && j != i) term = (float)v * (float)cur[j];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
-                float s2f = (float)alpha2 / lii;
-                s2 = (double)s2f;
-                mu = (double)(-term / lii);
-            }
-            if (lane == 0) {
-                double v1 = vn[i];
-                double y;
-                if (!MIXED) {
-                    double sq = sqrt(2.0 * s2), pdfn = sqrt(2.0 * pi * s2);
-                    double x = mu + v1 * sqrt(s2);
-                    double fx = (1.0 + erf((x - mu) / sq)) / 2.0;
-                    double f1 = (1.0 + erf((a.max_slip - mu) / sq)) / 2.0;
-                    double f0 = (1.0 + erf((0.0 - mu) / sq)) / 2.0;
-                    double target = (f1 - f0) * fx + f0;
-                    y = mu;
-                    double err = 1.0, yp = y + err;
-                    int cnt = 0;
-                    while (err > 1e-8 && cnt < 100) {
-                        double cdf = (1.0 + erf((y - mu) / sq)) / 2.0;
-                        double pdf = exp(-((y - mu) * (y - mu)) / (2.0 * s2)) / pdfn;
-                        y = y - (cdf - target) / pdf;
-                        err = fabs(y - yp);
-                        yp = y;
-                        ++cnt;
-                    }
-                    if (cnt >= 100) stat |= SMCGPU_ST_NEWTON_CAP;
-                } else {
-                    float sg = sqrtf((float)s2), muf = (float)mu;
-                    float al = (0.0f - muf) / sg, be = ((float)a.max_slip - muf) / sg;
-                    float u = normcdff((float)v1);
-                    float z;
-                    if (al >= 0.0f) {
-                        float qa = normcdff(-al), qb = normcdff(-be);
-                        float q = qa - u * (qa - qb);
-                        z = q > 0.0f ? -normcdfinvf(q) : al;
-                    } else {
-                        float pa = normcdff(al), pb = normcdff(be);
-                        float p = pa + u * (pb - pa);
-                        z = p > 0.0f ? normcdfinvf(p) : be;
-                    }
-                    float yf = muf + sg * z;
-                    yf = fminf(fmaxf(yf, 0.0f), (float)a.max_slip);
-                    y = (double)yf;
+        for (int lv = 0; lv < m.gb_nlevel; ++lv) {
+            const int q1 = m.gb_lvl_ptr[lv + 1];
+            for (int q = m.gb_lvl_ptr[lv] + lane; q < q1; q += 32) {
+                const int i = m.gb_order[q];
+                const int e0 = m.ll_ptr[i], e1 = m.ll_ptr[i + 1];
+                double lii = 0.0;
+                for (int e = e0; e < e1; ++e)
+                    if (m.ll_col[e] == i) lii = ll[e];
+                const double s2 = 1.0 / (lii / alpha2);
+                double mu = 0.0;
+                for (int e = e0; e < e1; ++e) {
+                    const int j = m.ll_col[e];
+                    if (j != i) mu = __dsub_rn(mu, __dmul_rn(__dmul_rn(ll[e] / alpha2, cur[j]), s2));
                 }
+                const double v1 = vn[i];
+                const double sq = sqrt(2.0 * s2), pdfn = sqrt(2.0 * pi * s2);
+                const double x = __dadd_rn(mu, __dmul_rn(v1, sqrt(s2)));
+                const double fx = (1.0 + erf((x - mu) / sq)) / 2.0;
+                const double f1 = (1.0 + erf((a.max_slip - mu) / sq)) / 2.0;
+                const double f0 = (1.0 + erf((0.0 - mu) / sq)) / 2.0;
+                const double target = __dadd_rn(__dmul_rn(f1 - f0, fx), f0);
+                double y = mu, err = 1.0, yp = y + err;
+                int cnt = 0;
+                while (err > 1e-8 && cnt < 100) {
+                    const double cdf = (1.0 + erf((y - mu) / sq)) / 2.0;
+                    const double pdf = exp(-__dmul_rn(y - mu, y - mu) / (2.0 * s2)) / pdfn;
+                    y = y - (cdf - target) / pdf;
+                    err = fabs(y - yp);
+                    yp = y;
+                    ++cnt;
+                }
+                if (cnt >= 100) stat |= SMCGPU_ST_NEWTON_CAP;
                 cur[i] = y;
             }
             __syncwarp();
@@ -113,6 +71,7 @@ __global__ void gibbs_kernel(MeshDev m, InnerArgs a) {
         for (int d = lane; d < D; d += 32) parts[(size_t)k * D + d] = cur[d];
         __syncwarp();
     }
+    stat = __reduce_or_sync(0xffffffffu, stat);
     if (lane == 0 && stat) atomicOr(a.status + th, stat);
 }
 
@@ -161,23 +120,25 @@ __global__ void gibbs_mixed_kernel(MeshDev m, InnerArgs a, int maxrow) {
             vn[2 * d2 + 1] = z.y;
         }
         __syncwarp();
-        for (int i = 0; i < D; ++i) {
-            float term = 0.0f;
-            if (lane < maxrow) {
-                const int j = rc[(size_t)i * maxrow + lane];
-                if (j >= 0) term = rv[(size_t)i * maxrow + lane] * cur[j];
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
-            if (lane == 0) {
+        // level by level, one component per lane (see gibbs_kernel)
+        for (int lv = 0; lv < m.gb_nlevel; ++lv) {
+            const int q1 = m.gb_lvl_ptr[lv + 1];
+            for (int q = m.gb_lvl_ptr[lv] + lane; q < q1; q += 32) {
+                const int i = m.gb_order[q];
+                float term = 0.0f;
+                for (int r = 0; r < maxrow; ++r) {
+                    const int j = rc[(size_t)i * maxrow + r];
+                    if (j < 0) break;
+                    term = fmaf(rv[(size_t)i * maxrow + r], cur[j], term);
+                }
                 const float muf = -term * ilii[i], sg = sgr[i];
                 const float al = (0.0f - muf) / sg, be = (mxs - muf) / sg;
                 const float u = normcdff(vn[i]);
                 float z;
                 if (al >= 0.0f) {
                     const float qa = normcdff(-al), qb = normcdff(-be);
-                    const float q = qa - u * (qa - qb);
-                    z = q > 0.0f ? -normcdfinvf(q) : al;
+                    const float qq = qa - u * (qa - qb);
+                    z = qq > 0.0f ? -normcdfinvf(qq) : al;
                 } else {
                     const float pa = normcdff(al), pb = normcdff(be);
                     const float p = pa + u * (pb - pa);
@@ -211,8 +172,8 @@ cudaError_t launch_gibbs(const MeshDev &m, const InnerArgs &a, cudaStream_t s) {
         if (e != cudaSuccess) return e;
         gibbs_mixed_kernel<<<(unsigned)((a.n_theta + w - 1) / w), w * 32, smm, s>>>(m, a, maxrow);
     } else {
-        cudaFuncSetAttribute(gibbs_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        gibbs_kernel<false><<<blocks, wpb * 32, sm, s>>>(m, a);
+        cudaFuncSetAttribute(gibbs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        gibbs_kernel<<<blocks, wpb * 32, sm, s>>>(m, a);
     }
     return cudaGetLastError();
 }

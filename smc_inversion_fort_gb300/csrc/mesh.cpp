@@ -204,6 +204,26 @@ std::string MeshPattern::build(const smcgpu_config &cfg) {
         ll_maxrow = std::max(ll_maxrow, (int)js.size());
     }
     if (ll_maxrow > LL_MAXNZ) return "L^T L row longer than LL_MAXNZ";
+    // levels of the Gibbs sweep (slip_gen_init_particles, smc_slip.f90:207-263):
+    // component i is updated after every coupled component j < i and before
+    // every coupled j > i; level(i) = 1 + max level of its coupled j < i, so
+    // updating level by level, the components of one level in any order,
+    // reproduces the sequential sweep exactly
+    {
+        std::vector<int> level(D, 0);
+        int nlevel = D > 0 ? 1 : 0;
+        for (int i = 0; i < D; ++i) {
+            for (int e = ll_ptr[i]; e < ll_ptr[i + 1]; ++e)
+                if (ll_col[e] < i) level[i] = std::max(level[i], level[ll_col[e]] + 1);
+            nlevel = std::max(nlevel, level[i] + 1);
+        }
+        gb_lvl_ptr.assign(nlevel + 1, 0);
+        for (int i = 0; i < D; ++i) ++gb_lvl_ptr[level[i] + 1];
+        for (int l = 0; l < nlevel; ++l) gb_lvl_ptr[l + 1] += gb_lvl_ptr[l];
+        gb_order.assign(D, 0);
+        std::vector<int> fill(gb_lvl_ptr.begin(), gb_lvl_ptr.end() - 1);
+        for (int i = 0; i < D; ++i) gb_order[fill[level[i]]++] = i;
+    }
     gauss_legendre(nquad, gq_x, gq_w);
     return "";
 }

@@ -34,6 +34,11 @@ struct MeshDev {
     const int *ll_ptr;        // [D+1] CSR of the structural pattern of L^T L
     const int *ll_col;        // [nnz]
     int ll_nnz, ll_maxrow;
+    // Gibbs sweep levels: components ordered by level (gb_order), level l holding
+    // gb_order[gb_lvl_ptr[l] .. gb_lvl_ptr[l+1]); no two components of a level are
+    // coupled by L^T L, and every coupled earlier component has a lower level
+    const int *gb_order, *gb_lvl_ptr;
+    int gb_nlevel;
     // observations
     const double *st_x, *st_y;      // [nstation]
     const int *st_row, *st_nrow;    // first row, 1 (SAR) or 3 (GNSS)
@@ -53,6 +58,7 @@ struct MeshPattern {
     std::vector<signed char> l_k, lt_k;
     std::vector<int> ll_ptr, ll_col;
     int ll_maxrow = 0;
+    std::vector<int> gb_order, gb_lvl_ptr;   // Gibbs sweep levels (see MeshDev)
     std::vector<double> gq_x, gq_w;
 
     // returns empty string on success
