@@ -173,18 +173,55 @@ def test_nested_mixed_matches_fp64(smcgpu, orc, engine):
     assert np.all(np.abs(np.median(a, 1) - np.median(b, 1)) < 4 * 1.2533 * se + 1e-9)
 
 
+def test_nested_mixed_latency_configuration_matches_fp64(smcgpu, orc):
+    """Batches no larger than the SM count run the MIXED warp-MMA engine with
+    16 warps and one geometry per CTA (larger batches: 8 warps, two geometries
+    per CTA).  Batches of 64 geometries against FP64, mean and median -log Z
+    over 192 streams within 4 standard errors."""
+    w, obs, o = setup_case("tiny", orc)
+    th = true_theta(w)
+    g64 = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
+    g64.set_data(obs)
+    g32 = smcgpu.SmcGpu(w.settings, smcgpu.PREC_MIXED)
+    g32.set_data(obs)
+    a, b = [], []
+    for r in range(3):
+        st = np.arange(64, dtype=np.uint64) + 6000 + 64 * r
+        va, sa = g64.fault_calc_likelihood(np.repeat(th[None], 64, 0), 23, st)
+        vb, sb = g32.fault_calc_likelihood(np.repeat(th[None], 64, 0), 23, st + 10**6)
+        assert np.all(sa == 0) and np.all(sb == 0)
+        a.append(va)
+        b.append(vb)
+    a, b = np.concatenate(a), np.concatenate(b)
+    se = np.sqrt((a.var(ddof=1) + b.var(ddof=1)) / len(a))
+    print("fp64", a.mean(), np.median(a), "mixed", b.mean(), np.median(b), "se", se)
+    assert abs(a.mean() - b.mean()) < 4 * se + 1e-9
+    assert abs(np.median(a) - np.median(b)) < 4 * 1.2533 * se + 1e-9
+
+
 def test_posterior_population(smcgpu, orc):
-    """Final inner population (the reference's slip output) against the oracle."""
+    """Final inner population (the reference's slip output) against the
+    oracle: per stream the two agree to rounding until a rounding-level
+    difference flips a discrete decision, so the posterior means are compared
+    over 12 independent streams, within 4 standard errors (+1e-3) per
+    component."""
     w, obs, o = setup_case("tiny", orc)
     th = true_theta(w)
     g = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
     g.set_data(obs)
-    got = g.fault_likelihood_posterior(th, 5, 77)
-    ref = o.fault_likelihood(th, 5, 77)
-    print("neglog", got["neglog"], ref["neglog"])
-    mg, mr = got["particles"].mean(0), ref["particles"].mean(0)
-    sd = ref["particles"].std(0) + 1e-3
-    assert np.all(np.abs(mg - mr) <= 0.5 * sd + 1e-9) or abs(got["neglog"] - ref["neglog"]) < 1e-7 * abs(ref["neglog"])
+    n = 12
+    mg, mr = [], []
+    for k in range(n):
+        got = g.fault_likelihood_posterior(th, 5, 77 + k)
+        ref = o.fault_likelihood(th, 5, 77 + k)
+        assert got["status"] == 0 and ref["status"] == 0
+        mg.append(got["particles"].mean(0))
+        mr.append(ref["particles"].mean(0))
+    mg, mr = np.array(mg), np.array(mr)
+    se = np.sqrt((mg.var(0, ddof=1) + mr.var(0, ddof=1)) / n)
+    diff = np.abs(mg.mean(0) - mr.mean(0))
+    print("max |diff|", diff.max(), "max se", se.max())
+    assert np.all(diff <= 4 * se + 1e-3)
 
 
 def test_gibbs_initial_population_matches_oracle(smcgpu, orc):
