@@ -939,13 +939,17 @@ extern "C" void orc_sigma_sar_inv(int32_t nobs, int32_t npath, const int32_t *ns
                 }
             double d = a[(size_t)c * n + c];
             for (int k = 0; k < n; ++k) { a[(size_t)k * n + c] /= d; inv[(size_t)k * n + c] /= d; }
-            for (int r = 0; r < n; ++r) {
-                if (r == c) continue;
-                double f = a[(size_t)c * n + r];
-                if (f == 0.0) continue;
-                for (int k = 0; k < n; ++k) {
-                    a[(size_t)k * n + r] -= f * a[(size_t)k * n + c];
-                    inv[(size_t)k * n + r] -= f * inv[(size_t)k * n + c];
+            // eliminate column c from every other row: row r -= f_r row c, with
+            // f_r = a(r, c) read before the update; columns outer, rows inner
+            // (contiguous), each element updated exactly as row by row
+            std::vector<double> f(a.begin() + (size_t)c * n, a.begin() + (size_t)(c + 1) * n);
+            for (int k = 0; k < n; ++k) {
+                const double akc = a[(size_t)k * n + c], ikc = inv[(size_t)k * n + c];
+                double *ak = &a[(size_t)k * n], *ik = &inv[(size_t)k * n];
+                for (int r = 0; r < n; ++r) {
+                    if (r == c || f[r] == 0.0) continue;
+                    ak[r] -= f[r] * akc;
+                    ik[r] -= f[r] * ikc;
                 }
             }
         }
