@@ -95,6 +95,7 @@ extern "C" int32_t smcgpu_create(const smcgpu_config *cfg, smcgpu_ctx **out) {
         e = "inner_engine must be SMCGPU_ENGINE_MMA, _CUDA or _TCGEN05";
     if (!e.empty()) { g_create_err = e; delete ctx; return SMCGPU_ERR_ARG; }
     cudaError_t ce = cudaSetDevice(cfg->device);
+    if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, cfg->device);
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
     for (int i = 0; i < 2 && ce == cudaSuccess; ++i) {

@@ -27,6 +27,7 @@ struct smcgpu_ctx {
     cudaStream_t own_stream = nullptr, copy_stream = nullptr, stream = nullptr;
     std::string err;
     bool has_data = false;
+    int nsm = 0;   // SMs of the device
     // host copy of the observation layout
     int nobs = 0, nsar = 0, ngnss = 0, npath = 0, nstation = 0;
     std::vector<int> nsar_index0;  // zero-based path starts, npath+1

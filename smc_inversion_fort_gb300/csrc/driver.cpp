@@ -435,8 +435,10 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
     smc::DevBuf<int> d_st;
     smc::DevBuf<unsigned long long> d_sid;
     std::vector<int32_t> stv;
+    // nested evaluations of a batch; the status bits of every evaluation are
+    // merged unless `used` marks the ones whose values are kept
     auto evaluate = [&](const std::vector<double> &th, const std::vector<unsigned long long> &sid,
-                        std::vector<double> &out) -> int {
+                        std::vector<double> &out, const std::vector<char> *used = nullptr) -> int {
         int nb = (int)sid.size();
         out.assign(nb, 0.0);
         if (nb == 0) return SMCGPU_OK;
@@ -450,7 +452,8 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
         CU(cudaMemcpyAsync(out.data(), d_nl.p, nb * sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
         CU(cudaMemcpyAsync(stv.data(), d_st.p, nb * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
         CU(cudaStreamSynchronize(s), "sync");
-        for (int q = 0; q < nb; ++q) status |= stv[q];
+        for (int q = 0; q < nb; ++q)
+            if (!used || (*used)[q]) status |= stv[q];
         return SMCGPU_OK;
     };
     double gamma = 0.0, evidence = 0.0;
@@ -576,24 +579,63 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
             }
         }
         // work_mcmc_sampling (smc_fault.f90:639-783): parents re-evaluated,
-        // then chained random-walk proposals, batched by chain position
+        // then chained random-walk proposals, batched by chain position.
+        // Step j + 1 of a chain starts from the outcome of step j, so the
+        // steps of a chain are sequential; late positions hold few chains and
+        // leave the GPU idle.  A batch therefore covers the K positions rr ..
+        // rr + K - 1 at once as each chain's decision tree: the proposal of a
+        // later step is formed for both outcomes of every earlier step in the
+        // window (2^m - 1 candidates for m steps), all are evaluated, and the
+        // Metropolis decisions then walk down the tree.  Proposals and
+        // evaluations are keyed by chain position, so the decisions, the
+        // kept values and every output equal the step-by-step run; the
+        // candidates off the taken path are discarded.
         std::vector<int32_t> start(N);
         start[0] = 0;
         for (int i = 0; i < N - 1; ++i) start[i + 1] = start[i] + assigned[i];
         std::vector<double> curp = parts, Lcur(N), newp((size_t)N * nd), newL(N), qcur = qs, newq(N, 0.0);
         int maxa = 0;
         for (int i = 0; i < N; ++i) maxa = std::max(maxa, (int)assigned[i]);
-        for (int rr = 0; rr < std::max(maxa, 1); ++rr) {
-            std::vector<int> who;
+        int nparents = 0;
+        for (int i = 0; i < N; ++i) nparents += assigned[i] > 0;
+        // batch size of a window of K positions from rr: 2^min(K, remaining) - 1 per chain
+        auto window_size = [&](int rr, int K) {
+            long long n = rr == 0 ? nparents : 0;
+            for (int i = 0; i < N; ++i) {
+                const int m = std::min(K, (int)assigned[i] - rr);
+                if (m > 0) n += (1LL << m) - 1;
+            }
+            return n;
+        };
+        // widen the window while the batch stays within one wave of the inner
+        // kernel (two geometries per SM) or within the unwidened batch
+        const long long wave = 2LL * std::max(ctx->nsm, 1);
+        auto proposal = [&](const double *from, int j, double *x) {
+            std::vector<double> z(nd);
+            for (int d = 0; d < nd; ++d) z[d] = host_normal(seed, OS, smc::RNG_OUT_PROP, iter, j, d);
+            trmv_lower(cov.data(), nd, z.data());
+            for (int d = 0; d < nd; ++d) x[d] = from[d] + z[d];
+            for (int d = 0; d < nd; ++d) {
+                double lo = range[2 * d], hi = range[2 * d + 1];
+                if (hi - lo > 1e-3) {
+                    if (x[d] < lo) x[d] = std::min(2.0 * lo - x[d], hi);
+                    if (x[d] > hi) x[d] = std::max(2.0 * hi - x[d], lo);
+                }
+            }
+        };
+        for (int rr = 0; rr < std::max(maxa, 1);) {
+            int K = 1;
+            const long long n1 = window_size(rr, 1);
+            while (K < 8 && rr + K < maxa && window_size(rr, K + 1) <= std::max(wave, n1)) ++K;
             std::vector<double> cand;
             std::vector<unsigned long long> sid;
             std::vector<int> pidx;
             if (rr == 0) {
                 // the parents' re-evaluation (smc_fault.f90:695-707) does not
                 // depend on any Metropolis decision, so it shares the first
-                // round's batch: parents first, then their first proposals.
-                // Parents without children are skipped: their value is never
-                // used (the reference computes and discards it).
+                // batch: parents first, then the proposals.  Parents without
+                // children are skipped: their value is never used (the
+                // reference computes and discards it).
                 for (int i = 0; i < N; ++i) {
                     if (assigned[i] == 0) continue;
                     pidx.push_back(i);
@@ -602,44 +644,71 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
                 }
             }
             const size_t npar = sid.size();
+            // per chain: its first candidate index and its window depth; node
+            // (l, b) of the tree is candidate first + 2^l - 1 + b, where bit t
+            // of b is the outcome (1: accepted) of step rr + t
+            std::vector<int> who, first, depth;
             for (int i = 0; i < N; ++i) {
-                if (assigned[i] <= rr) continue;
-                int j = start[i] + rr;
-                std::vector<double> z(nd), x(nd);
-                for (int d = 0; d < nd; ++d) z[d] = host_normal(seed, OS, smc::RNG_OUT_PROP, iter, j, d);
-                trmv_lower(cov.data(), nd, z.data());
-                for (int d = 0; d < nd; ++d) x[d] = curp[(size_t)i * nd + d] + z[d];
-                for (int d = 0; d < nd; ++d) {
-                    double lo = range[2 * d], hi = range[2 * d + 1];
-                    if (hi - lo > 1e-3) {
-                        if (x[d] < lo) x[d] = std::min(2.0 * lo - x[d], hi);
-                        if (x[d] > hi) x[d] = std::max(2.0 * hi - x[d], lo);
+                const int m = std::min(K, (int)assigned[i] - rr);
+                if (m <= 0) continue;
+                who.push_back(i);
+                first.push_back((int)(sid.size() - npar));
+                depth.push_back(m);
+                const size_t base = sid.size();
+                cand.resize(cand.size() + (((size_t)1 << m) - 1) * nd);
+                sid.resize(sid.size() + ((size_t)1 << m) - 1);
+                for (int l = 0; l < m; ++l) {
+                    const int j = start[i] + rr + l;
+                    for (int b = 0; b < (1 << l); ++b) {
+                        // the chain state before step rr + l on path b: the candidate
+                        // of the last accepted step on the path, else the current state
+                        const double *from = &curp[(size_t)i * nd];
+                        for (int t = l - 1; t >= 0; --t)
+                            if ((b >> t) & 1) {
+                                from = &cand[(base + ((size_t)1 << t) - 1 + (b & ((1 << t) - 1))) * nd];
+                                break;
+                            }
+                        const size_t node = base + ((size_t)1 << l) - 1 + b;
+                        proposal(from, j, &cand[node * nd]);
+                        sid[node] = smc::eval_stream(iter, 1, j);
                     }
                 }
-                who.push_back(i);
-                cand.insert(cand.end(), x.begin(), x.end());
-                sid.push_back(smc::eval_stream(iter, 1, j));
             }
             std::vector<double> Lall;
-            r = evaluate(cand, sid, Lall);
+            std::vector<char> used(sid.size(), 0);   // filled below; statuses merged after the walk
+            r = evaluate(cand, sid, Lall, &used);
             if (r) return r;
-            for (size_t q = 0; q < npar; ++q) Lcur[pidx[q]] = Lall[q];
-            for (size_t q = 0; q < who.size(); ++q) {
-                int i = who[q], j = start[i] + rr;
-                double Lq = Lall[npar + q];
-                double mh = smc::rng_uniform(seed, OS, smc::RNG_OUT_MH, iter, j, 0);
-                // work_mcmc_sampling's test (smc_fault.f90:748-771)
-                const double qc = gq ? neglog_q(*gq, &cand[(npar + q) * nd], nd) : 0.0;
-                const double lhs = gq ? gamma * (Lcur[i] - Lq) + (1.0 - gamma) * (qcur[i] - qc) : gamma * (Lcur[i] - Lq);
-                if (lhs > std::log(mh)) {
-                    for (int d = 0; d < nd; ++d) curp[(size_t)i * nd + d] = cand[(npar + q) * nd + d];
-                    Lcur[i] = Lq;
-                    qcur[i] = qc;
-                }
-                newL[j] = Lcur[i];
-                newq[j] = qcur[i];
-                for (int d = 0; d < nd; ++d) newp[(size_t)j * nd + d] = curp[(size_t)i * nd + d];
+            for (size_t q = 0; q < npar; ++q) {
+                Lcur[pidx[q]] = Lall[q];
+                used[q] = 1;
             }
+            for (size_t w2 = 0; w2 < who.size(); ++w2) {
+                const int i = who[w2];
+                int b = 0;
+                for (int l = 0; l < depth[w2]; ++l) {
+                    const int j = start[i] + rr + l;
+                    const size_t node = npar + (size_t)first[w2] + ((size_t)1 << l) - 1 + b;
+                    used[node] = 1;
+                    const double *c = &cand[node * nd];
+                    const double Lq = Lall[node];
+                    double mh = smc::rng_uniform(seed, OS, smc::RNG_OUT_MH, iter, j, 0);
+                    // work_mcmc_sampling's test (smc_fault.f90:748-771)
+                    const double qc = gq ? neglog_q(*gq, c, nd) : 0.0;
+                    const double lhs = gq ? gamma * (Lcur[i] - Lq) + (1.0 - gamma) * (qcur[i] - qc) : gamma * (Lcur[i] - Lq);
+                    if (lhs > std::log(mh)) {
+                        for (int d = 0; d < nd; ++d) curp[(size_t)i * nd + d] = c[d];
+                        Lcur[i] = Lq;
+                        qcur[i] = qc;
+                        b |= 1 << l;
+                    }
+                    newL[j] = Lcur[i];
+                    newq[j] = qcur[i];
+                    for (int d = 0; d < nd; ++d) newp[(size_t)j * nd + d] = curp[(size_t)i * nd + d];
+                }
+            }
+            for (size_t q = 0; q < used.size(); ++q)
+                if (used[q]) status |= stv[q];
+            rr += K;
         }
         parts = newp;
         Ls = newL;
