@@ -75,18 +75,24 @@ __global__ void gibbs_kernel(MeshDev m, InnerArgs a) {
     if (lane == 0 && stat) atomicOr(a.status + th, stat);
 }
 
-// MIXED: the same sweep in FP32 with the geometry's L^T L rows cached in
-// shared memory (off-diagonal columns and values, the diagonal, the
-// conditional standard deviation), so that a component update is one
-// shared-memory gather per lane, a warp sum and lane 0's inverse CDF.
+// MIXED: the same level-by-level sweep in FP32 with the geometry's L^T L
+// rows cached in shared memory (off-diagonal columns and values, the
+// diagonal, the conditional standard deviation): a component update is one
+// lane's row sum out of shared memory and its FP32 inverse CDF.
 __global__ void gibbs_mixed_kernel(MeshDev m, InnerArgs a, int maxrow) {
     extern __shared__ __align__(16) unsigned char gsm[];
     const int wpb = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int th = blockIdx.x * wpb + wid;
-    if (th >= a.n_theta) return;
     const int D = a.D, N = a.N, D2 = (D + 1) & ~1;
     const size_t per = (size_t)D * maxrow * 8 + (size_t)(2 * D2 + 2 * D) * 4;
     unsigned char *base = gsm + (size_t)wid * ((per + 15) & ~(size_t)15);
+    // the sweep's level tables, shared by the block's warps (loaded by every
+    // thread of the block before any warp leaves)
+    int *ord = (int *)(gsm + (size_t)wpb * ((per + 15) & ~(size_t)15)), *lvl = ord + D;
+    for (int q = threadIdx.x; q < D; q += blockDim.x) ord[q] = m.gb_order[q];
+    for (int q = threadIdx.x; q <= m.gb_nlevel; q += blockDim.x) lvl[q] = m.gb_lvl_ptr[q];
+    __syncthreads();
+    if (th >= a.n_theta) return;
     int *rc = (int *)base;                          // [D][maxrow] off-diagonal columns (-1: none)
     float *rv = (float *)(rc + (size_t)D * maxrow); // [D][maxrow] values
     float *cur = rv + (size_t)D * maxrow, *vn = cur + D2, *ilii = vn + D2, *sgr = ilii + D;
@@ -120,16 +126,20 @@ __global__ void gibbs_mixed_kernel(MeshDev m, InnerArgs a, int maxrow) {
             vn[2 * d2 + 1] = z.y;
         }
         __syncwarp();
-        // level by level, one component per lane (see gibbs_kernel)
+        // level by level, one component per lane (see gibbs_kernel); the row
+        // sum runs without branches (padding entries add an exact zero) so
+        // that its loads can be issued ahead of the FMA chain
         for (int lv = 0; lv < m.gb_nlevel; ++lv) {
-            const int q1 = m.gb_lvl_ptr[lv + 1];
-            for (int q = m.gb_lvl_ptr[lv] + lane; q < q1; q += 32) {
-                const int i = m.gb_order[q];
+            const int q1 = lvl[lv + 1];
+            for (int q = lvl[lv] + lane; q < q1; q += 32) {
+                const int i = ord[q];
+                const int *ri = rc + (size_t)i * maxrow;
+                const float *vi = rv + (size_t)i * maxrow;
                 float term = 0.0f;
+#pragma unroll 4
                 for (int r = 0; r < maxrow; ++r) {
-                    const int j = rc[(size_t)i * maxrow + r];
-                    if (j < 0) break;
-                    term = fmaf(rv[(size_t)i * maxrow + r], cur[j], term);
+                    const int j = ri[r];
+                    term = fmaf(vi[r], j >= 0 ? cur[j] : 0.0f, term);
                 }
                 const float muf = -term * ilii[i], sg = sgr[i];
                 const float al = (0.0f - muf) / sg, be = (mxs - muf) / sg;
@@ -166,8 +176,9 @@ cudaError_t launch_gibbs(const MeshDev &m, const InnerArgs &a, cudaStream_t s) {
         int dev = 0, maxsm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        const int w = (int)std::max<size_t>(1, std::min<size_t>(4, (size_t)maxsm / per));
-        const size_t smm = per * w;
+        const size_t tables = (size_t)(a.D + m.gb_nlevel + 1) * sizeof(int);
+        const int w = (int)std::max<size_t>(1, std::min<size_t>(4, ((size_t)maxsm - tables) / per));
+        const size_t smm = per * w + tables;
         cudaError_t e = cudaFuncSetAttribute(gibbs_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smm);
         if (e != cudaSuccess) return e;
         gibbs_mixed_kernel<<<(unsigned)((a.n_theta + w - 1) / w), w * 32, smm, s>>>(m, a, maxrow);
