@@ -12,24 +12,34 @@
 // draws are addressed by (stage, purpose, child index, dimension), so the
 // slot schedule does not change results.
 //
-// Two step engines share the stage-level code (bisection, normalisation,
+// Three step engines share the stage-level code (bisection, normalisation,
 // moments, resampling counts, parent queue, step-size tuning):
 //
-//  * CUDA cores (FP64, and MIXED with D > 128): every warp of a group owns
-//    C = 8 slots and runs its own FMA GEMM M x out of shared memory (lane l
-//    owns rows (l%16)*RT.. and slots (l/16)*4..), so a step needs no
-//    synchronisation beyond the warp.  W = 1..8 warps per geometry, chosen
-//    from the batch size.
+//  * CUDA cores (FP64 up to D = 128; MIXED up to 192 on request): every warp
+//    of a group owns C = 8 slots and runs its own FMA GEMM M x out of shared
+//    memory (lane l owns rows (l%16)*RT.. and slots (l/16)*4..), so a step
+//    needs no synchronisation beyond the warp.  W = 1..8 warps per geometry,
+//    chosen from the batch size.
 //
-//  * Tensor cores (MIXED, D <= 128): one warpgroup per geometry.  M is split
-//    into BF16 hi + lo (stacked 128/DP times to fill the 128-row MMA) and the
-//    slot tile's offsets from the stage mean likewise; thread 0 issues
+//  * Warp-level tensor-core MMA (MIXED default, D <= 256): M and the slots'
+//    offsets from the stage mean are split into BF16 hi + lo and multiplied
+//    with mma.sync m16n8k16 as lo*hi + hi*lo + hi*hi in three FP32 chains;
+//    each warp owns (16-row, 8-slot) tiles of a 16-warp (or 8-warp, two
+//    geometries per CTA) group.  Up to D = 128 M sits in shared memory (in
+//    registers for the stage when it is small); above, M is kept in global
+//    memory in fragment order and every warp streams its rows through a
+//    cp.async ring (Layout::AGL).
+//
+//  * tcgen05 (MIXED, D <= 128, on request): one warpgroup per geometry.  M
+//    is split into BF16 hi + lo (stacked 128/DP times to fill the 128-row
+//    MMA) and the slot tile's offsets likewise; thread 0 issues
 //    hi*hi + hi*lo + lo*hi as tcgen05.mma (M = 128, N = 2048/DP slots, K = 16
 //    per instruction) into a tensor-memory accumulator, and every thread
-//    reads back its row (one dimension) for 16 slots with tcgen05.ld.  The
-//    gradient error is O(2^-16) relative; the Metropolis test is exact for
-//    any deterministic gradient, and the end-point energies keep their FP32 /
-//    FP64 form, so only the acceptance rate can move.
+//    reads back its row (one dimension) for 16 slots with tcgen05.ld.
+//
+// The tensor-core gradient error is O(2^-16) relative; the Metropolis test
+// is exact for any deterministic gradient, and the end-point energies keep
+// their FP32 / FP64 form, so only the acceptance rate can move.
 //
 // FP64 (T = double) follows the reference's algebra in FP64.  MIXED
 // (T = float) runs the leapfrog in FP32 (or the tensor cores) about the stage
