@@ -42,6 +42,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-nested", action="store_true")
     p.add_argument("--no-c2", action="store_true", help="skip the c2 (D = 256) nested sample")
+    p.add_argument("--c2-cpu-baseline", action="store_true",
+                   help="also time the oracle on c2 (16 geometries, one per host thread: about 2.5 minutes, the "
+                        "slowest geometry sets the wall time)")
     p.add_argument("--outer-stages", type=int, default=1)
     return p.parse_args()
 
@@ -255,7 +258,8 @@ def nested_c2_bench(pkg, torch, cpu=True):
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     g.close()
-    out = {}
+    out = {} if cpu else {"cpu_baseline": None,
+                          "cpu_baseline_note": "off by default (about 2.5 minutes); bench.py --c2-cpu-baseline"}
     if cpu:
         # the oracle on all host threads, one geometry per thread, on the first
         # geometries of the same sample (the oracle's covariance set-up, like
@@ -436,7 +440,7 @@ def gb300_arm(args):
         line["nested_smc"] = nested_bench(pkg, torch, stages=args.outer_stages,
                                           cpu=(rank == 0 and not args.no_cpu_baseline))
         if not args.no_c2:
-            line["nested_smc_c2"] = nested_c2_bench(pkg, torch, cpu=(rank == 0 and not args.no_cpu_baseline))
+            line["nested_smc_c2"] = nested_c2_bench(pkg, torch, cpu=(rank == 0 and args.c2_cpu_baseline))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
