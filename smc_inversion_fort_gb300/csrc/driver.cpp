@@ -113,6 +113,8 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
         a.lv32 = ctx->d_lv32.p;
         a.ll32 = ctx->d_ll32.p;
         a.afrag = afrag_per_theta(ctx) ? ctx->d_afrag.p : nullptr;
+        CU(ctx->d_queue.ensure(1), "alloc queue");
+        a.queue = ctx->d_queue.p;
         a.warps_per_theta = ctx->cfg.inner_warps;
         a.engine = ctx->cfg.inner_engine;
         cudaError_t e = smc::launch_inner(ctx->md, a, s, &why);

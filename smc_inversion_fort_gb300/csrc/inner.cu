@@ -1850,15 +1850,43 @@ __global__ void __launch_bounds__(ENG == ENG_MMA ? 512 : 256) inner_group_kernel
         tc::fence_after_sync();
         tmem_base = tmem_slot;
     }
-    const int th = blockIdx.x * G + grp.id;
-    if (grp.id < G && th < a.n_theta)
-        group_body<T, RT, ENG, WG>(m, a, grp, th, smem_all + (size_t)grp.id * Layout<T, RT, ENG>::bytes(W), tmem_base);
+    if (grp.id < G) {
+        unsigned char *gsm = smem_all + (size_t)grp.id * Layout<T, RT, ENG>::bytes(W);
+        if (ENG == ENG_TC || !a.queue) {
+            const int th = blockIdx.x * G + grp.id;
+            if (th < a.n_theta) group_body<T, RT, ENG, WG>(m, a, grp, th, gsm, tmem_base);
+        } else {
+            // persistent groups: a group takes the next geometry from the
+            // queue when it finishes one, so uneven geometries balance at the
+            // granularity of one geometry (not of a CTA's G geometries)
+            __shared__ int next_th[8];
+            while (true) {
+                if (grp.gt == 0) next_th[grp.id] = atomicAdd(a.queue, 1);
+                grp.sync();
+                const int th = next_th[grp.id];
+                grp.sync();
+                if (th >= a.n_theta) break;
+                group_body<T, RT, ENG, WG>(m, a, grp, th, gsm, tmem_base);
+                grp.sync();
+            }
+        }
+    }
     if constexpr (ENG == ENG_TC) {
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
         if (warp == 0) tc::tmem_dealloc(tmem_base, ncols);
     }
+}
+
+// CTAs of a persistent launch: one wave (resident CTAs), no more than the
+// geometries need; the queue counter is reset on the launch's stream.
+// Without a queue, one CTA per G geometries.
+static unsigned persistent_blocks(const InnerArgs &a, int G, int resident, cudaStream_t s) {
+    const int need = (a.n_theta + G - 1) / G;
+    if (!a.queue) return (unsigned)need;
+    if (cudaMemsetAsync(a.queue, 0, sizeof(int), s) != cudaSuccess) return 0;
+    return (unsigned)std::max(1, std::min(need, resident));
 }
 
 template <typename T, int RT>
@@ -1887,7 +1915,11 @@ static cudaError_t launch_cc_t(const MeshDev &m, const InnerArgs &a, cudaStream_
     cudaError_t e = cudaFuncSetAttribute(inner_group_kernel<T, RT, ENG_CC, 0>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    unsigned blocks = (unsigned)((a.n_theta + G - 1) / G);
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, inner_group_kernel<T, RT, ENG_CC, 0>, 32 * W * G, sm);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = persistent_blocks(a, G, nsm * std::max(occ, 1), s);
+    if (!blocks) return cudaGetLastError();
     inner_group_kernel<T, RT, ENG_CC, 0><<<blocks, 32 * W * G, sm, s>>>(m, a, W, G);
     return cudaGetLastError();
 }
@@ -1909,7 +1941,14 @@ static cudaError_t launch_wg_t(const MeshDev &m, const InnerArgs &a, cudaStream_
     cudaError_t e = cudaFuncSetAttribute(inner_group_kernel<float, RT, ENG, WG>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    const unsigned blocks = (unsigned)((a.n_theta + G - 1) / G);
+    unsigned blocks = (unsigned)((a.n_theta + G - 1) / G);
+    if (ENG != ENG_TC) {
+        int occ = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, inner_group_kernel<float, RT, ENG, WG>, 32 * WG * G, sm);
+        if (e != cudaSuccess) return e;
+        blocks = persistent_blocks(a, G, nsm * std::max(occ, 1), s);
+        if (!blocks) return cudaGetLastError();
+    }
     inner_group_kernel<float, RT, ENG, WG><<<blocks, 32 * WG * G, sm, s>>>(m, a, WG, G);
     return cudaGetLastError();
 }

@@ -23,6 +23,7 @@ struct InnerArgs {
     float *lv32;          // [th][nrow][9] FP32 copy of the L values (MIXED), written by the inner kernel
     float *ll32;          // [th][ll_nnz] FP32 copy of the L^T L values (MIXED), written by the inner kernel
     uint4 *afrag;         // [th][256 * 256 / 4] stage matrix in MMA-fragment order (MIXED, 128 < D <= 256)
+    int *queue;           // device counter of the persistent launch (nullptr: one CTA per G geometries)
     const double *b;      // [th][D]
     const double *dsd;    // [th]
     const double *lval;   // [th][nrow][9] values of L (columns in MeshDev::l_col)

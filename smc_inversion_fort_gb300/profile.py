@@ -17,7 +17,8 @@ import numpy as np
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("what", choices=["greens", "nested"])
+    p.add_argument("what", choices=["greens", "nested", "outer"])
+    p.add_argument("--stages", type=int, default=1, help="outer: outer SMC stages after the initial evaluation")
     p.add_argument("--n-theta", type=int, default=0)
     p.add_argument("--fp32", action="store_true")
     p.add_argument("--mixed", action="store_true")
@@ -48,6 +49,26 @@ def main(argv=None):
             g.greens_dev(n, th.data_ptr(), out.data_ptr(), prec)
             torch.cuda.synchronize()
             print(f"greens n_theta={n} {'fp32' if a.fp32 else 'fp64'}: {1e3 * (time.perf_counter() - t0):.2f} ms")
+    elif a.what == "outer":
+        # fault_smc_exec on the workload's outer population, a few stages
+        from smc_inversion_fort_gb300.configs import prior_range
+        import dataclasses
+        w = preset(a.workload)
+        rng = np.random.default_rng(2024)
+        obs = make_stations(w, rng)
+        obs["dvec"] = np.zeros(len(obs["obs_sigma"]))
+        prec = pkg.PREC_MIXED if a.mixed else pkg.PREC_FP64
+        g = pkg.SmcGpu(w.settings, prec)
+        g.set_data(obs)
+        G = g.calc_greens_func(true_theta(w)[None])[0]
+        obs["dvec"] = G.T @ true_slip(w) + rng.standard_normal(G.shape[1]) * obs["obs_sigma"]
+        g.close()
+        g = pkg.SmcGpu(dataclasses.replace(w.settings, max_outer_stages=a.stages), prec)
+        g.set_data(obs)
+        t0 = time.perf_counter()
+        _, _, ev, ns = g.fault_smc_exec(prior_range(w), w.n_outer, 17)
+        print(f"outer {a.workload} {'mixed' if a.mixed else 'fp64'} {ns} stages: {time.perf_counter() - t0:.3f} s, "
+              f"evidence {ev:.4f}")
     else:
         w = preset(a.workload)
         w.settings.inner_warps = a.warps
