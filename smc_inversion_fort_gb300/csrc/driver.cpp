@@ -434,26 +434,55 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
     std::vector<int32_t> assigned(N), sorted(N);
     int status = 0;
     smc::DevBuf<double> d_th, d_nl;
-    smc::DevBuf<int> d_st;
+    smc::DevBuf<int> d_st, d_ns;
     smc::DevBuf<unsigned long long> d_sid;
-    std::vector<int32_t> stv;
+    std::vector<int32_t> stv, nsv;
+    // Inner stage count of each particle's latest evaluation: the cost key
+    // that orders a batch (not part of the snapshot; a resumed run starts
+    // unordered, which changes no result)
+    std::vector<int> Ns(N, 0);
     // nested evaluations of a batch; the status bits of every evaluation are
-    // merged unless `used` marks the ones whose values are kept
+    // merged unless `used` marks the ones whose values are kept.  With `key`,
+    // the batch runs in descending key order (the inner kernel's persistent
+    // groups then take the costliest geometries first); results come back in
+    // the caller's order, and the evaluations do not depend on the order.
     auto evaluate = [&](const std::vector<double> &th, const std::vector<unsigned long long> &sid,
-                        std::vector<double> &out, const std::vector<char> *used = nullptr) -> int {
+                        std::vector<double> &out, const std::vector<char> *used = nullptr,
+                        const std::vector<int> *key = nullptr, std::vector<int> *ns_out = nullptr) -> int {
         int nb = (int)sid.size();
         out.assign(nb, 0.0);
+        if (ns_out) ns_out->assign(nb, 0);
         if (nb == 0) return SMCGPU_OK;
-        stv.assign(nb, 0);
-        CU(d_th.upload(th.data(), th.size(), s), "upload");
-        CU(d_sid.upload(sid.data(), sid.size(), s), "upload");
+        std::vector<int> perm(nb);
+        for (int q = 0; q < nb; ++q) perm[q] = q;
+        if (key) std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return (*key)[x] > (*key)[y]; });
+        std::vector<double> th2((size_t)nb * nd);
+        std::vector<unsigned long long> sid2(nb);
+        for (int q = 0; q < nb; ++q) {
+            std::memcpy(&th2[(size_t)q * nd], &th[(size_t)perm[q] * nd], nd * sizeof(double));
+            sid2[q] = sid[perm[q]];
+        }
+        std::vector<double> out2(nb);
+        std::vector<int32_t> st2(nb), ns2(nb);
+        CU(d_th.upload(th2.data(), th2.size(), s), "upload");
+        CU(d_sid.upload(sid2.data(), sid2.size(), s), "upload");
         CU(d_nl.ensure(nb), "alloc");
         CU(d_st.ensure(nb), "alloc");
-        int rr = nested_batch(ctx, nb, d_th.p, seed, d_sid.p, d_nl.p, d_st.p, NestedOpts());
+        CU(d_ns.ensure(nb), "alloc");
+        NestedOpts opt;
+        opt.nstage = d_ns.p;
+        int rr = nested_batch(ctx, nb, d_th.p, seed, d_sid.p, d_nl.p, d_st.p, opt);
         if (rr) return rr;
-        CU(cudaMemcpyAsync(out.data(), d_nl.p, nb * sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
-        CU(cudaMemcpyAsync(stv.data(), d_st.p, nb * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+        CU(cudaMemcpyAsync(out2.data(), d_nl.p, nb * sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
+        CU(cudaMemcpyAsync(st2.data(), d_st.p, nb * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
+        CU(cudaMemcpyAsync(ns2.data(), d_ns.p, nb * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
         CU(cudaStreamSynchronize(s), "sync");
+        stv.assign(nb, 0);
+        for (int q = 0; q < nb; ++q) {
+            out[perm[q]] = out2[q];
+            stv[perm[q]] = st2[q];
+            if (ns_out) (*ns_out)[perm[q]] = ns2[q];
+        }
         for (int q = 0; q < nb; ++q)
             if (!used || (*used)[q]) status |= stv[q];
         return SMCGPU_OK;
@@ -496,7 +525,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
     {
         std::vector<unsigned long long> sid(N);
         for (int i = 0; i < N; ++i) sid[i] = smc::eval_stream(0, 0, i);
-        r = evaluate(parts, sid, Ls);
+        r = evaluate(parts, sid, Ls, nullptr, nullptr, &Ns);
         if (r) return r;
         // work_eval_init_particles (smc_fault.f90:350-353)
         if (gq)
@@ -569,6 +598,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
         {
             std::vector<int32_t> ta = assigned;
             std::vector<double> tp = parts, tl = Ls, tq = qs;
+            std::vector<int> tn = Ns;
             for (int i = 0; i < N; ++i) sorted[i] = i + 1;
             int32_t nn = N;
             smcgpu_qsort_(assigned.data(), sorted.data(), &nn);
@@ -578,6 +608,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
                 for (int d = 0; d < nd; ++d) parts[(size_t)k * nd + d] = tp[(size_t)org * nd + d];
                 Ls[k] = tl[org];
                 qs[k] = tq[org];
+                Ns[k] = tn[org];
             }
         }
         // work_mcmc_sampling (smc_fault.f90:639-783): parents re-evaluated,
@@ -596,6 +627,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
         start[0] = 0;
         for (int i = 0; i < N - 1; ++i) start[i + 1] = start[i] + assigned[i];
         std::vector<double> curp = parts, Lcur(N), newp((size_t)N * nd), newL(N), qcur = qs, newq(N, 0.0);
+        std::vector<int> curN = Ns, newN(N, 0);
         int maxa = 0;
         for (int i = 0; i < N; ++i) maxa = std::max(maxa, (int)assigned[i]);
         int nparents = 0;
@@ -646,6 +678,8 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
                 }
             }
             const size_t npar = sid.size();
+            std::vector<int> ckey;
+            for (size_t q = 0; q < npar; ++q) ckey.push_back(Ns[pidx[q]]);
             // per chain: its first candidate index and its window depth; node
             // (l, b) of the tree is candidate first + 2^l - 1 + b, where bit t
             // of b is the outcome (1: accepted) of step rr + t
@@ -659,6 +693,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
                 const size_t base = sid.size();
                 cand.resize(cand.size() + (((size_t)1 << m) - 1) * nd);
                 sid.resize(sid.size() + ((size_t)1 << m) - 1);
+                ckey.resize(sid.size(), curN[i]);
                 for (int l = 0; l < m; ++l) {
                     const int j = start[i] + rr + l;
                     for (int b = 0; b < (1 << l); ++b) {
@@ -678,10 +713,12 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
             }
             std::vector<double> Lall;
             std::vector<char> used(sid.size(), 0);   // filled below; statuses merged after the walk
-            r = evaluate(cand, sid, Lall, &used);
+            std::vector<int> nsall;
+            r = evaluate(cand, sid, Lall, &used, &ckey, &nsall);
             if (r) return r;
             for (size_t q = 0; q < npar; ++q) {
                 Lcur[pidx[q]] = Lall[q];
+                curN[pidx[q]] = nsall[q];
                 used[q] = 1;
             }
             for (size_t w2 = 0; w2 < who.size(); ++w2) {
@@ -701,10 +738,12 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
                         for (int d = 0; d < nd; ++d) curp[(size_t)i * nd + d] = c[d];
                         Lcur[i] = Lq;
                         qcur[i] = qc;
+                        curN[i] = nsall[node];
                         b |= 1 << l;
                     }
                     newL[j] = Lcur[i];
                     newq[j] = qcur[i];
+                    newN[j] = curN[i];
                     for (int d = 0; d < nd; ++d) newp[(size_t)j * nd + d] = curp[(size_t)i * nd + d];
                 }
             }
@@ -715,6 +754,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
         parts = newp;
         Ls = newL;
         qs = newq;
+        Ns = newN;
         if (output_dir) write_stage_csv(output_dir, iter, parts, Ls, N, nd);
         save_state(iter);
         iter = iter + 1;
