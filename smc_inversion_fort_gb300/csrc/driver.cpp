@@ -642,7 +642,10 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
             return n;
         };
         // widen the window while the batch stays within one wave of the inner
-        // kernel (two geometries per SM) or within the unwidened batch
+        // kernel (two geometries per SM) or within the unwidened batch, or
+        // while the added candidates are at most one wave: they cost at most
+        // one more geometry time in a batch that already spans several waves,
+        // and save a later batch, which costs at least its slowest geometry
         const long long wave = 2LL * std::max(ctx->nsm, 1);
         auto proposal = [&](const double *from, int j, double *x) {
             std::vector<double> z(nd);
@@ -660,7 +663,11 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
         for (int rr = 0; rr < std::max(maxa, 1);) {
             int K = 1;
             const long long n1 = window_size(rr, 1);
-            while (K < 8 && rr + K < maxa && window_size(rr, K + 1) <= std::max(wave, n1)) ++K;
+            while (K < 8 && rr + K < maxa) {
+                const long long nk = window_size(rr, K), nk1 = window_size(rr, K + 1);
+                if (nk1 > std::max(wave, n1) && nk1 - nk > wave) break;
+                ++K;
+            }
             std::vector<double> cand;
             std::vector<unsigned long long> sid;
             std::vector<int> pidx;
