@@ -135,6 +135,16 @@ int32_t smcgpu_set_stream(smcgpu_ctx *ctx, void *stream);
 /* Dimensions: ndim_fault, D = 2*ndof (nodal) or 2*npatch, nobs, nrow_l. */
 int32_t smcgpu_dims(const smcgpu_ctx *ctx, int32_t *ndim_fault, int32_t *D, int32_t *nobs, int32_t *nrow_l);
 
+/* Diagnostic, no reference counterpart; host only, needs no GPU.  The sweep
+ * schedule of the Gibbs initialisation (slip_gen_init_particles,
+ * smc_slip.f90:207-263) for a configuration: the D slip components ordered by
+ * level (order, 0-based) and the level starts (level_ptr, nlevel + 1 entries).
+ * No two components of a level are coupled by L^T L, and every coupled
+ * component j < i has a lower level than i, so a level-by-level sweep equals
+ * the sequential one.  With order == NULL only *D and *nlevel are returned. */
+int32_t smcgpu_gibbs_levels(const smcgpu_config *cfg, int32_t *D, int32_t *nlevel, int32_t *order,
+                            int32_t *level_ptr);
+
 /* Green's matrices for n_theta geometries: gmat(nobs, D, n_theta), the
  * reference's gmat(nobs, 2*ndof) per theta (gfunc.f90:242-348).  precision
  * SMCGPU_PREC_FP64 writes double, SMCGPU_PREC_FP32 writes float.

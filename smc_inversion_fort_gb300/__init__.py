@@ -81,6 +81,7 @@ def load_library() -> C.CDLL:
         "smcgpu_greens_batch": (i32, [vp, i32, vp, i32, vp]),
         "smcgpu_greens_batch_dev": (i32, [vp, i32, vp, i32, vp]),
         "smcgpu_gram_batch": (i32, [vp, i32, vp, vp, vp, vp]),
+        "smcgpu_gibbs_levels": (i32, [P(SmcConfig), vp, vp, vp, vp]),
         "smcgpu_fault_likelihood_batch": (i32, [vp, i32, vp, u64, vp, vp, vp]),
         "smcgpu_fault_likelihood_batch_dev": (i32, [vp, i32, vp, u64, vp, vp, vp]),
         "smcgpu_fault_likelihood_trace": (i32, [vp, i32, vp, u64, vp, vp, vp, vp, vp, vp]),
@@ -114,7 +115,7 @@ def load_library() -> C.CDLL:
 
 EXPORTED_SYMBOLS = [
     "smcgpu_default_config", "smcgpu_create", "smcgpu_destroy", "smcgpu_set_data", "smcgpu_set_stream",
-    "smcgpu_dims", "smcgpu_greens_batch", "smcgpu_greens_batch_dev", "smcgpu_gram_batch",
+    "smcgpu_dims", "smcgpu_gibbs_levels", "smcgpu_greens_batch", "smcgpu_greens_batch_dev", "smcgpu_gram_batch",
     "smcgpu_fault_likelihood_batch",
     "smcgpu_fault_likelihood_batch_dev", "smcgpu_fault_likelihood_trace", "smcgpu_fault_likelihood_posterior",
     "smcgpu_fault_smc_exec", "smcgpu_fault_smc_exec_gsmc", "smcgpu_fault_smc_resume", "smcgpu_resample_counts",
@@ -132,6 +133,23 @@ def _ptr(a: np.ndarray) -> int:
 
 class SmcError(RuntimeError):
     pass
+
+
+def gibbs_levels(s: SmcSettings):
+    """The Gibbs sweep schedule of a configuration (host only): a list of
+    levels, each the 0-based slip components updated together."""
+    lib = load_library()
+    cfg = make_config(s)
+    D, nl = C.c_int32(), C.c_int32()
+    rc = lib.smcgpu_gibbs_levels(C.byref(cfg), C.byref(D), C.byref(nl), None, None)
+    if rc != 0:
+        raise SmcError(f"smcgpu_gibbs_levels failed ({rc})")
+    order = np.zeros(max(D.value, 1), np.int32)
+    ptr = np.zeros(nl.value + 1, np.int32)
+    rc = lib.smcgpu_gibbs_levels(C.byref(cfg), C.byref(D), C.byref(nl), _ptr(order), _ptr(ptr))
+    if rc != 0:
+        raise SmcError(f"smcgpu_gibbs_levels failed ({rc})")
+    return [order[ptr[k]:ptr[k + 1]].tolist() for k in range(nl.value)]
 
 
 def make_config(s: SmcSettings, precision: int = PREC_FP64, device: int = 0) -> SmcConfig:

@@ -75,6 +75,20 @@ static void refresh_md(smcgpu_ctx *ctx) {
     m.nsar_index = ctx->d_nsar_index.p; m.sar_inv = ctx->d_sar_w.p; m.sar_off = ctx->d_sar_off.p;
 }
 
+extern "C" int32_t smcgpu_gibbs_levels(const smcgpu_config *cfg, int32_t *D, int32_t *nlevel, int32_t *order,
+                                       int32_t *level_ptr) {
+    if (!cfg || !D || !nlevel || (order && !level_ptr)) return SMCGPU_ERR_ARG;
+    smc::MeshPattern p;
+    if (!p.build(*cfg).empty()) return SMCGPU_ERR_ARG;
+    *D = p.D;
+    *nlevel = (int32_t)p.gb_lvl_ptr.size() - 1;
+    if (order) {
+        std::copy(p.gb_order.begin(), p.gb_order.end(), order);
+        std::copy(p.gb_lvl_ptr.begin(), p.gb_lvl_ptr.end(), level_ptr);
+    }
+    return SMCGPU_OK;
+}
+
 extern "C" int32_t smcgpu_create(const smcgpu_config *cfg, smcgpu_ctx **out) {
     g_create_err.clear();
     if (!cfg || !out) { g_create_err = "null argument"; return SMCGPU_ERR_ARG; }
