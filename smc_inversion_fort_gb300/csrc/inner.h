@@ -44,4 +44,16 @@ struct InnerArgs {
 cudaError_t launch_gibbs(const MeshDev &m, const InnerArgs &a, cudaStream_t s);
 cudaError_t launch_inner(const MeshDev &m, const InnerArgs &a, cudaStream_t s, const char **why);
 
+// engine families behind launch_inner, one translation unit each
+cudaError_t launch_inner_fp64(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W);           // D <= 128
+cudaError_t launch_inner_fp64_96(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W);        // 64 < D <= 96
+cudaError_t launch_inner_fp64_128(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W);       // 96 < D <= 128
+cudaError_t launch_inner_cc32(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W);           // D <= 192
+cudaError_t launch_inner_cc32_wide(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W);      // 64 < D <= 192
+cudaError_t launch_inner_cc32_192(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W);       // 128 < D <= 192
+cudaError_t launch_inner_mma_wide(const MeshDev &m, const InnerArgs &a, cudaStream_t s);              // D <= 128
+cudaError_t launch_inner_mma_pair(const MeshDev &m, const InnerArgs &a, cudaStream_t s);              // D <= 128
+cudaError_t launch_inner_mma_streamed(const MeshDev &m, const InnerArgs &a, cudaStream_t s);          // 128 < D <= 256
+cudaError_t launch_inner_tc(const MeshDev &m, const InnerArgs &a, cudaStream_t s);                    // D <= 128
+
 }  // namespace smc

@@ -1,0 +1,10 @@
+// Inner SMC, MIXED CUDA-core engine, 192-row tile (128 < D <= 192).
+#include "inner_impl.cuh"
+
+namespace smc {
+
+cudaError_t launch_inner_cc32_192(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W) {
+    return launch_cc_t<float, 12>(m, a, s, W);
+}
+
+}  // namespace smc

@@ -1,0 +1,13 @@
+// Inner SMC, tcgen05 engine instantiations (D <= 128).
+#include "inner_impl.cuh"
+
+namespace smc {
+
+cudaError_t launch_inner_tc(const MeshDev &m, const InnerArgs &a, cudaStream_t s) {
+    const int D = a.D;
+    if (D <= 32) return launch_wg_t<2, ENG_TC, 4>(m, a, s, 2);
+    if (D <= 64) return launch_wg_t<4, ENG_TC, 4>(m, a, s, 2);
+    return launch_wg_t<8, ENG_TC, 4>(m, a, s, 2);
+}
+
+}  // namespace smc
