@@ -28,7 +28,8 @@ UNIT = "GF entries/s"
 # Algorithmic FP64 operations per unique (theta, patch, Gauss point, station)
 # evaluation of the displacement-only DC3D0 for both slip directions
 # (fault-frame offsets 7, UB0 displacement terms 75 incl. 1 sqrt + 2 div,
-# quadrature weight and 6 accumulations 15): see the design doc.
+# quadrature weight and 6 accumulations 15), counted from greens.cu's
+# dc3d0 displacement terms.
 FLOPS_PER_EVAL = 97
 
 

@@ -4,8 +4,8 @@
  * Every entry point is extern "C", takes plain pointers and sizes, returns an
  * int32_t status (SMCGPU_OK = 0) and never exits, stops or traps.  Arrays are
  * in the reference's Fortran layouts (column-major, first index fastest), so a
- * Fortran caller passes its own arrays through ISO_C_BINDING unchanged; the
- * `bind(C)` interface module is shown in INTEGRATION.md.  Host pointers are
+ * Fortran caller passes its own arrays through ISO_C_BINDING unchanged (a
+ * `bind(C)` interface per entry point, as for sort.cpp's qsort_).  Host pointers are
  * owned by the caller and not retained past a call.  One context drives one
  * GPU; calls on a context must be serialised by the caller.
  *
@@ -52,6 +52,9 @@ extern "C" {
 #define SMCGPU_ST_TUNE_COUNT  32   /* step-size resampling count != N                  */
 #define SMCGPU_ST_WAIT_CAP    64   /* a bounded device wait (tensor-core completion)
                                       gave up; the evaluation was abandoned, neglog = 1e10 */
+#define SMCGPU_ST_SNAPSHOT_IO 128   /* fault_smc_exec: a stage snapshot (<iter>.state) could
+                                      not be written; the run itself is unaffected, but it
+                                      cannot be resumed from that stage                 */
 
 /* theta layouts */
 #define SMCGPU_LAYOUT_TRACE          0  /* [ymin ymax (x_i y_i)_{i<nplane} dip_1..n la2 ls_sar ls_gnss] (init.f90:152-167) */
@@ -172,7 +175,10 @@ int32_t smcgpu_gram_batch(smcgpu_ctx *ctx, int32_t n_theta, const double *theta,
  * must be <= 16384, otherwise SMCGPU_ERR_ARG.  No cudaMalloc, cudaFree or
  * allocating library call is made.  The first call on a device looks up the
  * array's address (cudaGetSymbolAddress) and should come before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race. */
+ * capture.  The address is cached per device for the life of the process:
+ * after cudaDeviceReset (or any teardown of the device's primary context) it
+ * is stale, so do not call this entry point again in that process.  All calls
+ * share the array: calls that overlap on the GPU race. */
 int32_t smcgpu_greens_batch_noalloc(smcgpu_ctx *ctx, int32_t n_theta, const double *theta_dev,
                                     int32_t precision, void *gmat_dev);
 
@@ -323,6 +329,29 @@ int32_t smcgpu_write_point_cloud(smcgpu_ctx *ctx, const char *prefix, int32_t n,
 /* Last error message of the context (or, when ctx is NULL, of the last
  * create call or file reader on this thread). */
 const char *smcgpu_last_error(const smcgpu_ctx *ctx);
+
+/* ---- run statistics (no counterpart in the reference, which prints only the
+ * wall time of one nested evaluation, main.f90:464-480) ----
+ * smcgpu_stats_reset clears the counters and turns recording on (enable != 0)
+ * or off.  While on, every nested batch records device events around its
+ * inner SMC launch and around the whole batch (Green's build to inner SMC),
+ * and the inner kernel adds its tempering stages and HMC trajectories to two
+ * device counters.  smcgpu_stats_get synchronises the context's stream and
+ * returns the totals since the reset. */
+typedef struct smcgpu_stats {
+    int64_t nested_evals;        /* geometries evaluated                                  */
+    int64_t inner_stages;        /* tempering stages, summed over evaluations             */
+    int64_t inner_trajectories;  /* HMC trajectories (tuning + sampling), summed          */
+    double inner_kernel_ms;      /* device time of the inner SMC launches                 */
+    double nested_ms;            /* device time of the nested batches                      */
+} smcgpu_stats;
+int32_t smcgpu_stats_reset(smcgpu_ctx *ctx, int32_t enable);
+int32_t smcgpu_stats_get(smcgpu_ctx *ctx, smcgpu_stats *out);
+/* Per-stage timing of the last smcgpu_fault_smc_exec / _gsmc / _resume call
+ * (always recorded, host wall clock): seconds[k] and evals[k] for k = 0 (the
+ * initial population's evaluation; absent after a resume) and the stages
+ * 1..nstage; up to max entries are written, *n_out gets the number recorded. */
+int32_t smcgpu_outer_stage_times(smcgpu_ctx *ctx, int32_t max, double *seconds, int64_t *evals, int32_t *n_out);
 
 #ifdef __cplusplus
 }

@@ -24,6 +24,7 @@ BASIS_NODAL, BASIS_PATCH = 0, 1
 PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
 ST_BISECT_CAP, ST_STAGE_CAP, ST_NONFINITE, ST_NEWTON_CAP, ST_REFLECT_CAP, ST_TUNE_COUNT = 1, 2, 4, 8, 16, 32
 ST_WAIT_CAP = 64
+ST_SNAPSHOT_IO = 128
 ENGINE_MMA, ENGINE_CUDA, ENGINE_TCGEN05 = 0, 1, 2
 
 
@@ -42,6 +43,12 @@ class SmcConfig(C.Structure):
         ("precision", C.c_int32), ("device", C.c_int32), ("max_outer_stages", C.c_int32),
         ("inner_warps", C.c_int32), ("inner_engine", C.c_int32),
     ]
+
+
+class Stats(C.Structure):
+    """smcgpu_stats: totals since smcgpu_stats_reset."""
+    _fields_ = [("nested_evals", C.c_int64), ("inner_stages", C.c_int64), ("inner_trajectories", C.c_int64),
+                ("inner_kernel_ms", C.c_double), ("nested_ms", C.c_double)]
 
 
 PATH_MAX = 512
@@ -104,6 +111,9 @@ def load_library() -> C.CDLL:
         "smcgpu_write_slip_map": (i32, [vp, C.c_char_p, i32, vp]),
         "smcgpu_point_cloud": (i32, [vp, i32, vp, vp, i32, vp]),
         "smcgpu_write_point_cloud": (i32, [vp, C.c_char_p, i32, i32, vp]),
+        "smcgpu_stats_reset": (i32, [vp, i32]),
+        "smcgpu_stats_get": (i32, [vp, P(Stats)]),
+        "smcgpu_outer_stage_times": (i32, [vp, i32, vp, vp, P(i32)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -123,7 +133,7 @@ EXPORTED_SYMBOLS = [
     "smcgpu_last_error", "smcgpu_read_settings", "smcgpu_settings_to_config", "smcgpu_count_observations",
     "smcgpu_read_observations", "smcgpu_read_range", "smcgpu_read_values", "smcgpu_write_slip",
     "smcgpu_slip_map", "smcgpu_slip_to_nodes", "smcgpu_write_slip_map", "smcgpu_point_cloud",
-    "smcgpu_write_point_cloud",
+    "smcgpu_write_point_cloud", "smcgpu_stats_reset", "smcgpu_stats_get", "smcgpu_outer_stage_times",
 ]
 
 
@@ -222,6 +232,25 @@ class SmcGpu:
         self._check(self.lib.smcgpu_set_data(self.h, len(dv), _ptr(pts), _ptr(e), _ptr(sg), _ptr(dv), npath,
                                              _ptr(idx), int(obs["ngnss"])), "set_data")
         self.nobs = len(dv)
+
+    def stats_reset(self, enable: bool = True):
+        """Clear the run statistics and turn their recording on or off."""
+        self._check(self.lib.smcgpu_stats_reset(self.h, 1 if enable else 0), "stats_reset")
+
+    def stats(self) -> dict:
+        st = Stats()
+        self._check(self.lib.smcgpu_stats_get(self.h, C.byref(st)), "stats_get")
+        return {f: getattr(st, f) for f, _ in Stats._fields_}
+
+    def outer_stage_times(self):
+        """(seconds, evaluations) per stage of the last fault_smc_exec; entry 0
+        is the initial population's evaluation."""
+        n = C.c_int32()
+        self._check(self.lib.smcgpu_outer_stage_times(self.h, 0, None, None, C.byref(n)), "outer_stage_times")
+        sec, ev = np.zeros(n.value), np.zeros(n.value, np.int64)
+        self._check(self.lib.smcgpu_outer_stage_times(self.h, n.value, _ptr(sec), _ptr(ev), C.byref(n)),
+                    "outer_stage_times")
+        return sec, ev
 
     def set_stream(self, stream_handle: int | None):
         self._check(self.lib.smcgpu_set_stream(self.h, stream_handle or None), "set_stream")

@@ -119,7 +119,38 @@ def preset(name: str) -> Workload:
         s = SmcSettings(layout=0, basis=0, nxi=(4,), neta=(3,), nquad=2, nparticle_slip=64,
                         xmin=-10.0, xmax=10.0, zmin=-10.0)
         return Workload("tiny-sar", s, 16, 8, 30, 2, 60.0, 0.2, 0.5, 1.0)
+    if name == "tiny-2plane":
+        # the reference's bent trace (init.f90:152-167): two planes meeting
+        # at a free bend point (x, y) in theta, nodal basis
+        s = SmcSettings(layout=0, basis=0, nplane=2, nxi=(3, 3), neta=(3, 3), nquad=2, nparticle_slip=64,
+                        xmin=-10.0, xmax=10.0, zmin=-10.0)
+        return Workload("tiny-2plane", s, 16, 12, 0, 0, 60.0, 0.2, 0.5, 1.0)
+    if name == "tiny-3plane-fix":
+        # fix_xbend = .true. (init.f90:135-150): three planes, bends at fixed
+        # x, their y in theta, uneven patch counts along strike
+        s = SmcSettings(layout=1, basis=0, nplane=3, nxi=(2, 3, 2), neta=(3, 3, 3), xbend=(-3.0, 4.0), nquad=2,
+                        nparticle_slip=64, xmin=-10.0, xmax=10.0, zmin=-10.0)
+        return Workload("tiny-3plane-fix", s, 16, 12, 0, 0, 60.0, 0.2, 0.5, 1.0)
+    if name == "tiny-2plane-sar":
+        # two planes with InSAR paths (exponential covariance) and GNSS
+        s = SmcSettings(layout=0, basis=0, nplane=2, nxi=(3, 3), neta=(3, 3), nquad=2, nparticle_slip=64,
+                        xmin=-10.0, xmax=10.0, zmin=-10.0)
+        return Workload("tiny-2plane-sar", s, 16, 8, 30, 2, 60.0, 0.2, 0.5, 1.0)
     raise KeyError(name)
+
+
+def _trace_truth(s: SmcSettings):
+    """Bend points of the synthetic trace: on the line from (xmin, -4) to
+    (xmax, 5) with an alternating 1.5 km offset; dips 50, 58, 66, ..."""
+    ymin, ymax = -4.0, 5.0
+    n = s.nplane
+    if s.layout == 1:
+        xb = np.asarray(s.xbend[: n - 1], dtype=np.float64)
+    else:
+        xb = s.xmin + (s.xmax - s.xmin) * np.arange(1, n) / n
+    yb = ymin + (ymax - ymin) * (xb - s.xmin) / (s.xmax - s.xmin) + 1.5 * (-1.0) ** np.arange(1, n)
+    dips = 50.0 + 8.0 * (np.arange(n) % 3)
+    return ymin, ymax, xb, yb, dips
 
 
 def true_theta(w: Workload) -> np.ndarray:
@@ -129,10 +160,15 @@ def true_theta(w: Workload) -> np.ndarray:
         if s.rect_hyper:
             t = np.concatenate([t, [0.0, 0.0]])
         return t
-    # trace layout, one plane: [ymin, ymax, dip, log a2, log s2_sar, log s2_gnss]
-    if s.layout == 0 and s.nplane == 1:
-        return np.array([-4.0, 5.0, 50.0, -3.0, 0.0, 0.0])
-    raise NotImplementedError("synthetic truth for this layout")
+    # trace layouts (init.f90:121-196): [ymin, ymax, bends, dip_1..n,
+    # log a2, log s2_sar, log s2_gnss]; bends are (x, y) pairs (layout 0) or
+    # the y of each fixed x bend (layout 1)
+    ymin, ymax, xb, yb, dips = _trace_truth(s)
+    if s.layout == 0:
+        bends = np.ravel(np.column_stack([xb, yb])) if s.nplane > 1 else np.zeros(0)
+    else:
+        bends = yb
+    return np.concatenate([[ymin, ymax], bends, dips, [-3.0, 0.0, 0.0]])
 
 
 def prior_range(w: Workload) -> np.ndarray:
@@ -142,9 +178,15 @@ def prior_range(w: Workload) -> np.ndarray:
         if s.rect_hyper:
             r = np.concatenate([r, [[-2.0, 2.0], [-2.0, 2.0]]])
         return r
-    if s.layout == 0 and s.nplane == 1:
-        return np.array([[-10.0, 2.0], [-2.0, 10.0], [20.0, 80.0], [-10.0, 2.0], [0.0, 0.0], [0.0, 0.0]])
-    raise NotImplementedError
+    ymin, ymax, xb, yb, dips = _trace_truth(s)
+    rows = [[-10.0, 2.0], [-2.0, 10.0]]
+    for k in range(s.nplane - 1):
+        if s.layout == 0:
+            rows.append([xb[k] - 2.0, xb[k] + 2.0])
+        rows.append([yb[k] - 3.0, yb[k] + 3.0])
+    rows += [[20.0, 80.0]] * s.nplane
+    rows += [[-10.0, 2.0], [0.0, 0.0], [0.0, 0.0]]
+    return np.array(rows)
 
 
 def make_stations(w: Workload, rng: np.random.Generator):
@@ -192,27 +234,34 @@ def make_stations(w: Workload, rng: np.random.Generator):
 
 
 def true_slip(w: Workload) -> np.ndarray:
-    """Gaussian-shaped slip, 1 m peak dip slip and 0.5 m strike slip."""
+    """Gaussian-shaped slip, 1 m peak dip slip and 0.5 m strike slip, over
+    the along-strike coordinate of the whole trace (all planes) and the
+    down-dip coordinate; in the DOF order of discretize_fault
+    (init.f90:198-293: per plane, node rows from the bottom edge up, no DOF
+    on the bottom edge or on the outer ends of the end planes) for the nodal
+    basis, patch order i + nxi*j per plane for the patch-constant basis."""
     s = w.settings
-    nxi, neta = s.nxi[0], s.neta[0]
-    if s.basis == 1:
-        u = (np.arange(nxi) + 0.5) / nxi
-        v = (np.arange(neta) + 0.5) / neta
-    else:
-        u = np.arange(nxi + 1) / nxi
-        v = np.arange(neta + 1) / neta
-    U, V = np.meshgrid(u, v)          # [row j][col i]
-    bump = np.exp(-((U - 0.5) ** 2 / (2 * 0.18 ** 2) + (V - 0.55) ** 2 / (2 * 0.25 ** 2)))
-    if s.basis == 1:
-        vals = bump.ravel()           # patch order i + nxi*j
-    else:
-        vals = []
-        for j in range(neta + 1):
-            for i in range(nxi + 1):
-                if j == 0 or i == 0 or i == nxi:
-                    continue
-                vals.append(bump[j, i])
-        vals = np.array(vals)
+    tot = sum(s.nxi[:s.nplane])
+
+    def bump(u, v):
+        return np.exp(-((u - 0.5) ** 2 / (2 * 0.18 ** 2) + (v - 0.55) ** 2 / (2 * 0.25 ** 2)))
+
+    vals = []
+    off = 0
+    for p in range(s.nplane):
+        nxi, neta = s.nxi[p], s.neta[p]
+        if s.basis == 1:
+            for j in range(neta):
+                for i in range(nxi):
+                    vals.append(bump((off + i + 0.5) / tot, (j + 0.5) / neta))
+        else:
+            for j in range(neta + 1):
+                for i in range(nxi + 1):
+                    if j == 0 or (p == 0 and i == 0) or (p == s.nplane - 1 and i == nxi):
+                        continue
+                    vals.append(bump((off + i) / tot, j / neta))
+        off += nxi
+    vals = np.array(vals)
     sl = np.zeros(2 * len(vals))
     sl[0::2] = 0.5 * vals
     sl[1::2] = 1.0 * vals

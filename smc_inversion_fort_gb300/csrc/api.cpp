@@ -153,6 +153,8 @@ extern "C" int32_t smcgpu_destroy(smcgpu_ctx *ctx) {
     cudaSetDevice(ctx->cfg.device);
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    for (cudaEvent_t e : ctx->stats.inner_ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->stats.batch_ev) cudaEventDestroy(e);
     for (int i = 0; i < 2; ++i) {
         if (ctx->ev_done[i]) cudaEventDestroy(ctx->ev_done[i]);
         if (ctx->ev_copied[i]) cudaEventDestroy(ctx->ev_copied[i]);
@@ -215,8 +217,15 @@ extern "C" int32_t smcgpu_set_data(smcgpu_ctx *ctx, int32_t nobs, const double *
         if (idx0[p + 1] < idx0[p]) return ctx->fail(SMCGPU_ERR_ARG, "set_data: nsar_index not monotone");
     int nsar = npath > 0 ? idx0[npath] : 0;
     if (nsar + 3 * ngnss != nobs) return ctx->fail(SMCGPU_ERR_ARG, "set_data: nobs != nsar_total + 3*ngnss");
-    for (int i = 0; i < nobs; ++i)
-        if (!(obs_sigma[i] > 0.0)) return ctx->fail(SMCGPU_ERR_ARG, "set_data: obs_sigma must be positive");
+    for (int i = 0; i < nobs; ++i) {
+        if (!(obs_sigma[i] > 0.0) || !std::isfinite(obs_sigma[i]))
+            return ctx->fail(SMCGPU_ERR_ARG, "set_data: obs_sigma must be positive and finite (row " +
+                                                 std::to_string(i + 1) + ")");
+        if (!std::isfinite(dvec[i]) || !std::isfinite(obs_points[2 * i]) || !std::isfinite(obs_points[2 * i + 1]) ||
+            !std::isfinite(obs_unitvec[3 * i]) || !std::isfinite(obs_unitvec[3 * i + 1]) ||
+            !std::isfinite(obs_unitvec[3 * i + 2]))
+            return ctx->fail(SMCGPU_ERR_ARG, "set_data: non-finite observation (row " + std::to_string(i + 1) + ")");
+    }
     ctx->nobs = nobs; ctx->nsar = nsar; ctx->ngnss = ngnss; ctx->npath = npath;
     ctx->nstation = nsar + ngnss;
     ctx->nsar_index0 = idx0;

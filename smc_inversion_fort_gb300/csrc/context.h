@@ -63,6 +63,19 @@ struct smcgpu_ctx {
     smc::DevBuf<int> d_counts, d_flag;
     cudaEvent_t ev_done[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
 
+    // run statistics (smcgpu_stats_*): off unless enabled; device event pairs
+    // around the inner kernel and the whole nested batch, resolved lazily
+    struct Stats {
+        bool on = false;
+        std::vector<cudaEvent_t> inner_ev, batch_ev;   // start, stop, start, stop, ...
+        double inner_ms = 0.0, batch_ms = 0.0;
+        long long evals = 0;
+        smc::DevBuf<unsigned long long> d_counters;    // [0] stages, [1] trajectories
+    } stats;
+    // per-stage wall seconds and nested evaluations of the last fault_smc_exec
+    std::vector<double> outer_stage_s;
+    std::vector<long long> outer_stage_evals;
+
     int fail(int code, const std::string &msg) {
         err = msg;
         return code;

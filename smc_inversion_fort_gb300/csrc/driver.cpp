@@ -3,6 +3,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdlib>
 #include <cmath>
 #include <cstdio>
@@ -53,6 +54,29 @@ size_t bytes_per_theta(const smcgpu_ctx *ctx) {
     return b;
 }
 
+// Run statistics: an event recorded on the stream, kept for later timing.
+cudaError_t stats_mark(std::vector<cudaEvent_t> &v, cudaStream_t s) {
+    cudaEvent_t e = nullptr;
+    cudaError_t r = cudaEventCreate(&e);
+    if (r != cudaSuccess) return r;
+    v.push_back(e);
+    return cudaEventRecord(e, s);
+}
+
+// Sums the (start, stop) pairs of v into ms and releases the events.
+cudaError_t stats_resolve(std::vector<cudaEvent_t> &v, double &ms) {
+    cudaError_t r = cudaSuccess;
+    for (size_t i = 0; i + 1 < v.size(); i += 2) {
+        float t = 0.0f;
+        if (r == cudaSuccess) r = cudaEventSynchronize(v[i + 1]);
+        if (r == cudaSuccess) r = cudaEventElapsedTime(&t, v[i], v[i + 1]);
+        ms += t;
+    }
+    for (cudaEvent_t e : v) cudaEventDestroy(e);
+    v.clear();
+    return r;
+}
+
 // Runs the nested evaluation for n thetas already on the device, in chunks.
 int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed, const unsigned long long *streams_dev,
                  double *neglog_dev, int *status_dev, const NestedOpts &opt) {
@@ -83,9 +107,18 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
     CU(ctx->d_ll32.ensure((size_t)chunk * std::max<size_t>(pm.ll_col.size(), 1)), "alloc ll32");
     if (afrag_per_theta(ctx)) CU(ctx->d_afrag.ensure((size_t)chunk * afrag_per_theta(ctx)), "alloc stage matrices");
     CU(ctx->d_nstage_tmp.ensure((size_t)chunk), "alloc");
+    auto &stats = ctx->stats;
+    if (stats.on && stats.inner_ev.size() > 4096) {
+        CU(stats_resolve(stats.inner_ev, stats.inner_ms), "stats");
+        CU(stats_resolve(stats.batch_ev, stats.batch_ms), "stats");
+    }
     for (int t0 = 0; t0 < n; t0 += chunk) {
         int nb = std::min(chunk, n - t0);
         const double *th = theta_dev + (size_t)t0 * nd;
+        if (stats.on) {
+            CU(stats_mark(stats.batch_ev, s), "stats event");
+            stats.evals += nb;
+        }
         CU(smc::launch_planes(ctx->md, nb, th, ctx->d_planes.p, s), "planes kernel");
         CU(smc::launch_greens(ctx->md, nb, ctx->d_planes.p, SMCGPU_PREC_FP64, ctx->d_gmat.p, s), "greens kernel");
         CU(smc::launch_setup(ctx->md, nb, th, ctx->d_planes.p, ctx->d_lval.p, ctx->d_ltval.p, ctx->d_llval.p,
@@ -117,11 +150,14 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
         a.queue = ctx->d_queue.p;
         a.warps_per_theta = ctx->cfg.inner_warps;
         a.engine = ctx->cfg.inner_engine;
+        a.counters = stats.on ? stats.d_counters.p : nullptr;
+        if (stats.on) CU(stats_mark(stats.inner_ev, s), "stats event");
         cudaError_t e = smc::launch_inner(ctx->md, a, s, &why);
         if (e != cudaSuccess) {
             if (why) return ctx->fail(SMCGPU_ERR_ARG, why);
             return ctx->cuda_fail(e, "inner kernel");
         }
+        if (stats.on) CU(stats_mark(stats.inner_ev, s), "stats event");
         if (opt.mean_dev)
             CU(smc::launch_mean_particles(nb, N, D, ctx->d_parts.p, opt.mean_dev + (size_t)t0 * D, s), "mean kernel");
         if (opt.particles_out && t0 == 0) {
@@ -132,6 +168,7 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
             CU(cudaMemcpyAsync(opt.prior_out, ctx->d_dbuf.p + N, (size_t)N * sizeof(double), cudaMemcpyDeviceToHost,
                                s), "copy");
         }
+        if (stats.on) CU(stats_mark(stats.batch_ev, s), "stats event");
     }
     return SMCGPU_OK;
 }
@@ -441,6 +478,18 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
     // that orders a batch (not part of the snapshot; a resumed run starts
     // unordered, which changes no result)
     std::vector<int> Ns(N, 0);
+    // per-stage wall time and evaluations (smcgpu_outer_stage_times)
+    ctx->outer_stage_s.clear();
+    ctx->outer_stage_evals.clear();
+    long long stage_evals = 0;
+    auto stage_t0 = std::chrono::steady_clock::now();
+    auto stage_done = [&]() {
+        const auto t1 = std::chrono::steady_clock::now();
+        ctx->outer_stage_s.push_back(std::chrono::duration<double>(t1 - stage_t0).count());
+        ctx->outer_stage_evals.push_back(stage_evals);
+        stage_evals = 0;
+        stage_t0 = t1;
+    };
     // nested evaluations of a batch; the status bits of every evaluation are
     // merged unless `used` marks the ones whose values are kept.  With `key`,
     // the batch runs in descending key order (the inner kernel's persistent
@@ -453,6 +502,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
         out.assign(nb, 0.0);
         if (ns_out) ns_out->assign(nb, 0);
         if (nb == 0) return SMCGPU_OK;
+        stage_evals += nb;
         std::vector<int> perm(nb);
         for (int q = 0; q < nb; ++q) perm[q] = q;
         if (key) std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return (*key)[x] > (*key)[y]; });
@@ -495,7 +545,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
         o.nd = nd; o.N = N; o.iter = it; o.gsmc = gq ? 1 : 0; o.status = status;
         o.gamma = gamma; o.evidence = evidence;
         o.parts = parts; o.Ls = Ls; o.qs = qs;
-        if (!write_state(output_dir, o)) status |= SMCGPU_ST_NONFINITE;
+        if (!write_state(output_dir, o)) status |= SMCGPU_ST_SNAPSHOT_IO;
     };
     if (resume) {
         parts = resume->parts;
@@ -533,6 +583,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
     }
     if (output_dir) write_stage_csv(output_dir, 0, parts, Ls, N, nd);
     save_state(0);
+    stage_done();
     }
     CU(ctx->d_w.ensure(N), "alloc");
     CU(ctx->d_counts.ensure(N), "alloc");
@@ -764,6 +815,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
         Ns = newN;
         if (output_dir) write_stage_csv(output_dir, iter, parts, Ls, N, nd);
         save_state(iter);
+        stage_done();
         iter = iter + 1;
         if (iter > 100000) break;
     }
@@ -866,5 +918,53 @@ extern "C" int32_t smcgpu_point_cloud(smcgpu_ctx *ctx, int32_t n_theta, const do
     CU(smc::launch_point_cloud(ctx->md, n_theta, d_pl.p, d_slip.p, stride, nr, d_pts.p, s), "point cloud kernel");
     CU(cudaMemcpyAsync(points_out, d_pts.p, npts * 6 * sizeof(double), cudaMemcpyDeviceToHost, s), "copy points");
     CU(cudaStreamSynchronize(s), "sync");
+    return SMCGPU_OK;
+}
+
+extern "C" int32_t smcgpu_stats_reset(smcgpu_ctx *ctx, int32_t enable) {
+    if (!ctx) return SMCGPU_ERR_ARG;
+    CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+    auto &st = ctx->stats;
+    double scratch = 0.0;
+    CU(cudaStreamSynchronize(ctx->stream), "sync");
+    CU(stats_resolve(st.inner_ev, scratch), "stats");
+    CU(stats_resolve(st.batch_ev, scratch), "stats");
+    st.inner_ms = st.batch_ms = 0.0;
+    st.evals = 0;
+    st.on = enable != 0;
+    if (st.on) {
+        CU(st.d_counters.ensure(2), "alloc counters");
+        CU(cudaMemsetAsync(st.d_counters.p, 0, 2 * sizeof(unsigned long long), ctx->stream), "memset");
+        CU(cudaStreamSynchronize(ctx->stream), "sync");
+    }
+    return SMCGPU_OK;
+}
+
+extern "C" int32_t smcgpu_stats_get(smcgpu_ctx *ctx, smcgpu_stats *out) {
+    if (!ctx || !out) return SMCGPU_ERR_ARG;
+    CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+    auto &st = ctx->stats;
+    CU(cudaStreamSynchronize(ctx->stream), "sync");
+    CU(stats_resolve(st.inner_ev, st.inner_ms), "stats");
+    CU(stats_resolve(st.batch_ev, st.batch_ms), "stats");
+    unsigned long long c[2] = {0, 0};
+    if (st.d_counters.p) CU(cudaMemcpy(c, st.d_counters.p, sizeof(c), cudaMemcpyDeviceToHost), "copy counters");
+    out->nested_evals = st.evals;
+    out->inner_stages = (int64_t)c[0];
+    out->inner_trajectories = (int64_t)c[1];
+    out->inner_kernel_ms = st.inner_ms;
+    out->nested_ms = st.batch_ms;
+    return SMCGPU_OK;
+}
+
+extern "C" int32_t smcgpu_outer_stage_times(smcgpu_ctx *ctx, int32_t max, double *seconds, int64_t *evals,
+                                            int32_t *n_out) {
+    if (!ctx || !n_out || max < 0) return SMCGPU_ERR_ARG;
+    const int n = (int)ctx->outer_stage_s.size();
+    for (int k = 0; k < std::min(n, (int)max); ++k) {
+        if (seconds) seconds[k] = ctx->outer_stage_s[k];
+        if (evals) evals[k] = ctx->outer_stage_evals[k];
+    }
+    *n_out = n;
     return SMCGPU_OK;
 }

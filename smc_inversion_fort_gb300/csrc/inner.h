@@ -39,6 +39,7 @@ struct InnerArgs {
     int *nstage;                 // [th]
     double *trace_gamma;         // optional [th][max_stages+2]
     double *trace_inc;           // optional [th][max_stages+2]
+    unsigned long long *counters;  // optional: [0] += tempering stages, [1] += HMC trajectories
 };
 
 cudaError_t launch_gibbs(const MeshDev &m, const InnerArgs &a, cudaStream_t s);

@@ -533,10 +533,21 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
         }
     }
     grp.sync();
+    // A geometry whose initial population has a non-finite likelihood or prior
+    // (a non-finite theta or observation, a degenerate plane) is abandoned with
+    // SMCGPU_ST_NONFINITE and neglog = NaN: the reference would carry the NaN
+    // through every stage.
+    bool nonfinite = false;
+    {
+        double bad = 0.0;
+        for (int k = gt; k < N; k += gnt) bad += (isfinite(Lc[k]) && isfinite(Pc[k])) ? 0.0 : 1.0;
+        nonfinite = grp.sum(bad) > 0.0;
+    }
 
     double gamma = 0.0, neglog = 0.0, log_up = 0.0, log_lo = -1e1;
+    double ntraj = 0.0;   // HMC trajectories run (tuning and sampling)
     int iter = 1;
-    while (1.0 - gamma > 10e-8) {
+    while (!nonfinite && 1.0 - gamma > 10e-8) {
         // ---- next tempering exponent (smc_slip.f90:314-387)
         double lmin = 1e300;
         for (int k = gt; k < N; k += gnt) lmin = fmin(lmin, Lc[k]);
@@ -607,6 +618,10 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
         }
         double ev = grp.sum(ps) / N;
         double inc = -log(ev) + dg * lmin;
+        if (!isfinite(inc)) {   // the weights of this stage are not finite
+            nonfinite = true;
+            break;
+        }
         gamma = g;
         neglog += inc;
         if (gt == 0 && a.trace_gamma) {
@@ -838,13 +853,16 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
             const bool tuning = pass == 0;
             const uint32_t P_MOM = tuning ? RNG_TUNE_MOM : RNG_SMP_MOM;
             const uint32_t P_MH = tuning ? RNG_TUNE_MH : RNG_SMP_MH;
-            double nql = 0.0;
+            double nql = 0.0, ntl = 0.0;
             for (int k = gt; k < NP2; k += gnt) {
                 bool ok = k < N && cnt[k] > 0 && (!tuning || k % a.tf == 0);
                 keys[k] = ok ? (int)(((unsigned)(N - cnt[k]) << 16) | (unsigned)k) : 0x7fffffff;
                 nql += ok;
+                ntl += ok ? cnt[k] : 0;   // one trajectory per child of a queued parent
             }
-            const int nq = (int)grp.sum(nql);
+            grp.sum2(nql, ntl);
+            const int nq = (int)nql;
+            ntraj += ntl;
             grp.sync();
             for (int size = 2; size <= NP2; size <<= 1)
                 for (int stride = size >> 1; stride > 0; stride >>= 1) {
@@ -1813,12 +1831,17 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
     for (int o = 16; o > 0; o >>= 1) status |= __shfl_xor_sync(FULL, status, o);
     if (lane == 0 && status) atomicOr(&gint[2], status);
     grp.sync();
+    if (nonfinite) neglog = __longlong_as_double(0x7ff8000000000000LL);   // NaN
     if (gt == 0) {
         int st = gint[2];
         if (!isfinite(neglog)) st |= SMCGPU_ST_NONFINITE;
         a.neglog[th] = neglog;
         atomicOr(a.status + th, st);
         a.nstage[th] = iter - 1;
+        if (a.counters) {
+            atomicAdd(a.counters, (unsigned long long)(iter - 1));
+            atomicAdd(a.counters + 1, (unsigned long long)ntraj);
+        }
     }
 }
 

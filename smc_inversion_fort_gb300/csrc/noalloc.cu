@@ -16,7 +16,9 @@
 //    every GPU that loads the library until the process exits);
 //  * the first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current); make that first call
-//    before any stream capture;
+//    before any stream capture.  The address is cached per device index for
+//    the life of the process, so it goes stale if the device's primary
+//    context is destroyed (cudaDeviceReset): no call may follow a reset;
 //  * every call shares the one array and it keeps the last call's records:
 //    calls whose launches overlap on the GPU race on it, so calls on one
 //    device must be ordered (same stream, or synchronised);

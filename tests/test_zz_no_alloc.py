@@ -8,7 +8,9 @@ lives in a fixed device array instead of a buffer grown with cudaMalloc.
 This test checks, on two calls in a row with different geometries, that its
 output equals smcgpu_greens_batch_dev's (the tolerance of the Green's tests,
 1e-12 of the column scale; the two share the kernels, so it is exact in
-practice), and that a batch larger than the fixed array is refused.
+practice), that repeated calls change neither the device's free memory nor
+torch's allocator statistics, and that a batch larger than the fixed array is
+refused.
 
 The file is named so that pytest collects it after every other test.
 """
@@ -57,6 +59,23 @@ def test_noalloc_greens_matches_allocating_path(smcgpu):
             a, b = out.double().cpu().numpy(), ref.double().cpu().numpy()
             assert np.isfinite(a).all()
             assert _colwise_rel(a, b) <= 1e-12
+    # the point of the entry point: after a warm-up call, further calls leave
+    # the device's free memory (cudaMemGetInfo) and torch's allocator untouched
+    n = 300
+    th = torch.from_numpy(random_thetas(w, n, seed=77)).cuda()
+    out = torch.empty((n, dm["D"], dm["nobs"]), dtype=torch.float64, device="cuda")
+    assert f(g.h, n, th.data_ptr(), smcgpu.PREC_FP64, out.data_ptr()) == 0
+    stream.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    stats0 = torch.cuda.memory_stats()
+    for _ in range(3):
+        assert f(g.h, n, th.data_ptr(), smcgpu.PREC_FP64, out.data_ptr()) == 0
+    stream.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    stats1 = torch.cuda.memory_stats()
+    assert free1 == free0, (free0, free1)
+    for k in ("allocation.all.allocated", "segment.all.allocated", "reserved_bytes.all.current"):
+        assert stats1.get(k) == stats0.get(k), k
     # batches beyond the fixed array are refused with a clear error
     big = torch.zeros((MAX_RECORDS + 1, dm["ndim_fault"]), dtype=torch.float64, device="cuda")
     rc = f(g.h, MAX_RECORDS + 1, big.data_ptr(), smcgpu.PREC_FP64, big.data_ptr())
