@@ -70,10 +70,14 @@ extern "C" {
 #define SMCGPU_PREC_FP32   1   /* Green's build only: FP32 arithmetic, float output    */
 #define SMCGPU_PREC_MIXED  2   /* nested SMC: FP32 leapfrog, FP64 likelihood/evidence  */
 
-/* inner SMC step engines (smcgpu_config.inner_engine, MIXED only) */
+/* inner SMC step engines (smcgpu_config.inner_engine) */
 #define SMCGPU_ENGINE_MMA      0   /* BF16x3 mma.sync tiles, FP32 accumulate (default)  */
 #define SMCGPU_ENGINE_CUDA     1   /* FP32 FMA on CUDA cores                            */
 #define SMCGPU_ENGINE_TCGEN05  2   /* BF16x3 tcgen05.mma with a tensor-memory accumulator */
+#define SMCGPU_ENGINE_GLOBAL   3   /* stage matrix in global memory, streamed once per
+                                      leapfrog step; any slip dimension up to 1024 (MIXED,
+                                      FP32 FMA) or 512 (FP64).  The other engines fall back
+                                      to it above their own limits.                     */
 
 typedef struct smcgpu_config {
     int32_t layout;
@@ -102,11 +106,14 @@ typedef struct smcgpu_config {
     int32_t inner_warps;           /* CUDA-core inner SMC engine: warps per geometry
                                       particle, 1, 2, 4 or 8; 0 picks from the batch size.
                                       Results do not depend on it.                      */
-    int32_t inner_engine;          /* MIXED leapfrog engine, SMCGPU_ENGINE_*: warp-level
+    int32_t inner_engine;          /* leapfrog engine, SMCGPU_ENGINE_*.  MIXED: warp-level
                                       tensor-core MMA (default; slip dimensions <= 256,
                                       the stage matrix streamed from global memory above
-                                      128), CUDA cores (<= 192), or tcgen05 (<= 128, CUDA
-                                      cores above).  FP64 takes slip dimensions <= 128.  */
+                                      128), CUDA cores (<= 192), tcgen05 (<= 128), or the
+                                      global-matrix engine (<= 1024; also the fallback
+                                      above each engine's limit).  FP64: CUDA cores up to
+                                      128, the global-matrix engine up to 512 (or at any
+                                      size with SMCGPU_ENGINE_GLOBAL).                  */
 } smcgpu_config;
 
 typedef struct smcgpu_ctx smcgpu_ctx;

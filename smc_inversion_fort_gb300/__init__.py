@@ -25,7 +25,7 @@ PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
 ST_BISECT_CAP, ST_STAGE_CAP, ST_NONFINITE, ST_NEWTON_CAP, ST_REFLECT_CAP, ST_TUNE_COUNT = 1, 2, 4, 8, 16, 32
 ST_WAIT_CAP = 64
 ST_SNAPSHOT_IO = 128
-ENGINE_MMA, ENGINE_CUDA, ENGINE_TCGEN05 = 0, 1, 2
+ENGINE_MMA, ENGINE_CUDA, ENGINE_TCGEN05, ENGINE_GLOBAL = 0, 1, 2, 3
 
 
 class SmcConfig(C.Structure):

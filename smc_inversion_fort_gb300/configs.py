@@ -39,7 +39,7 @@ class SmcSettings:
     sar_corr_len: float = 10.0
     max_outer_stages: int = 0
     inner_warps: int = 0          # GPU inner kernel: warps per geometry (0: by batch size)
-    inner_engine: int = 0         # MIXED inner step engine: 0 warp MMA, 1 CUDA cores, 2 tcgen05
+    inner_engine: int = 0         # inner step engine: 0 warp MMA, 1 CUDA cores, 2 tcgen05, 3 global matrix
 
     def ndim_fault(self) -> int:
         if self.layout == 0:
@@ -107,6 +107,13 @@ def preset(name: str) -> Workload:
     if name in ("d160", "d256"):   # parity cases above 128 slip dimensions (10x8 and 16x8 patches)
         nxi = 10 if name == "d160" else 16
         s = SmcSettings(layout=2, basis=1, nxi=(nxi,), neta=(8,), nquad=2, nparticle_slip=64, ntau=20)
+        return Workload(name, s, 16, 30, 0, 0, 60.0, 0.2, 0.5, 1.0)
+    if name in ("d512", "d544", "d1024", "d1056"):
+        # global-matrix engine sizes: 16x16, 17x16, 32x16 (the c4 slip size) and
+        # 33x16 patches; few inner particles and short trajectories so that the
+        # oracle finishes in seconds
+        nxi = {"d512": 16, "d544": 17, "d1024": 32, "d1056": 33}[name]
+        s = SmcSettings(layout=2, basis=1, nxi=(nxi,), neta=(16,), nquad=2, nparticle_slip=64, ntau=10)
         return Workload(name, s, 16, 30, 0, 0, 60.0, 0.2, 0.5, 1.0)
     if name == "tiny":      # parity case small enough for the oracle
         s = SmcSettings(layout=2, basis=1, nxi=(4,), neta=(2,), nquad=2, nparticle_slip=64)

@@ -105,8 +105,8 @@ extern "C" int32_t smcgpu_create(const smcgpu_config *cfg, smcgpu_ctx **out) {
     if (e.empty() && cfg->inner_warps != 0 && cfg->inner_warps != 1 && cfg->inner_warps != 2 &&
         cfg->inner_warps != 4 && cfg->inner_warps != 8)
         e = "inner_warps must be 0, 1, 2, 4 or 8";
-    if (e.empty() && (cfg->inner_engine < SMCGPU_ENGINE_MMA || cfg->inner_engine > SMCGPU_ENGINE_TCGEN05))
-        e = "inner_engine must be SMCGPU_ENGINE_MMA, _CUDA or _TCGEN05";
+    if (e.empty() && (cfg->inner_engine < SMCGPU_ENGINE_MMA || cfg->inner_engine > SMCGPU_ENGINE_GLOBAL))
+        e = "inner_engine must be SMCGPU_ENGINE_MMA, _CUDA, _TCGEN05 or _GLOBAL";
     if (!e.empty()) { g_create_err = e; delete ctx; return SMCGPU_ERR_ARG; }
     cudaError_t ce = cudaSetDevice(cfg->device);
     if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, cfg->device);

@@ -58,6 +58,7 @@ struct smcgpu_ctx {
     smc::DevBuf<float> d_A32, d_lv32, d_ll32;
     smc::DevBuf<int> d_queue;     // geometry queue of the persistent inner kernel
     smc::DevBuf<uint4> d_afrag;   // stage matrices in MMA-fragment order (MIXED, 128 < D <= 256)
+    smc::DevBuf<char> d_mgl, d_glxc;   // global-matrix engine: stage matrices, slot chain states
     smc::DevBuf<int> d_ibuf, d_nstage_tmp, d_nstage;
     smc::DevBuf<double> d_w;
     smc::DevBuf<int> d_counts, d_flag;

@@ -44,6 +44,18 @@ size_t afrag_per_theta(const smcgpu_ctx *ctx) {
     return streamed ? (size_t)256 * 256 / 4 : 0;
 }
 
+// global-matrix engine: bytes per geometry of the stage matrix and of the
+// slots' chain states (0 when another engine runs the batch)
+size_t gl_bytes_per_theta(const smcgpu_ctx *ctx, size_t *mgl, size_t *glxc) {
+    const int D = ctx->mesh.D;
+    const bool mixed = ctx->cfg.precision == SMCGPU_PREC_MIXED;
+    const size_t el = mixed ? sizeof(float) : sizeof(double);
+    const bool on = smc::inner_uses_global(mixed, ctx->cfg.inner_engine, D);
+    *mgl = on ? (size_t)D * D * el : 0;
+    *glxc = on ? (size_t)16 * D * el : 0;
+    return *mgl + *glxc;
+}
+
 size_t bytes_per_theta(const smcgpu_ctx *ctx) {
     const smc::MeshPattern &p = ctx->mesh;
     size_t D = p.D, N = ctx->cfg.nparticle_slip, NP2 = next_pow2((int)N);
@@ -51,6 +63,8 @@ size_t bytes_per_theta(const smcgpu_ctx *ctx) {
     b += (size_t)p.nrow * 9 * 8 + D * 9 * 8 + p.ll_col.size() * 8 + sizeof(smc::ThetaAux);
     b += 2 * N * D * 8 + 9 * N * 8 + 4 * NP2 * 4 + p.nplane * sizeof(smc::PlaneGeom) + 64;
     b += afrag_per_theta(ctx) * sizeof(uint4);
+    size_t m1, m2;
+    b += gl_bytes_per_theta(ctx, &m1, &m2);
     return b;
 }
 
@@ -106,6 +120,11 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
     CU(ctx->d_lv32.ensure((size_t)chunk * std::max(pm.nrow, 1) * 9), "alloc lv32");
     CU(ctx->d_ll32.ensure((size_t)chunk * std::max<size_t>(pm.ll_col.size(), 1)), "alloc ll32");
     if (afrag_per_theta(ctx)) CU(ctx->d_afrag.ensure((size_t)chunk * afrag_per_theta(ctx)), "alloc stage matrices");
+    size_t mgl_b = 0, glxc_b = 0;
+    if (gl_bytes_per_theta(ctx, &mgl_b, &glxc_b)) {
+        CU(ctx->d_mgl.ensure((size_t)chunk * mgl_b), "alloc global stage matrices");
+        CU(ctx->d_glxc.ensure((size_t)chunk * glxc_b), "alloc chain states");
+    }
     CU(ctx->d_nstage_tmp.ensure((size_t)chunk), "alloc");
     auto &stats = ctx->stats;
     if (stats.on && stats.inner_ev.size() > 4096) {
@@ -146,6 +165,8 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
         a.lv32 = ctx->d_lv32.p;
         a.ll32 = ctx->d_ll32.p;
         a.afrag = afrag_per_theta(ctx) ? ctx->d_afrag.p : nullptr;
+        a.mgl = mgl_b ? (void *)ctx->d_mgl.p : nullptr;
+        a.glxc = glxc_b ? (void *)ctx->d_glxc.p : nullptr;
         CU(ctx->d_queue.ensure(1), "alloc queue");
         a.queue = ctx->d_queue.p;
         a.warps_per_theta = ctx->cfg.inner_warps;

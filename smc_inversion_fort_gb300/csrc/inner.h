@@ -13,7 +13,7 @@ struct InnerArgs {
     int n_theta, N, NP2, D, mixed;
     int ntau, tf, max_stages;
     int warps_per_theta;  // CUDA-core engine: warps per geometry (1, 2, 4, 8; 0 picks by batch size)
-    int engine;           // MIXED step engine, SMCGPU_ENGINE_* (warp MMA: D <= 256, tcgen05: D <= 128)
+    int engine;           // step engine, SMCGPU_ENGINE_* (warp MMA: D <= 256, tcgen05: D <= 128, global: any)
     double cv, max_slip;
     uint64_t seed;
     const unsigned long long *streams;  // [n_theta]
@@ -23,6 +23,8 @@ struct InnerArgs {
     float *lv32;          // [th][nrow][9] FP32 copy of the L values (MIXED), written by the inner kernel
     float *ll32;          // [th][ll_nnz] FP32 copy of the L^T L values (MIXED), written by the inner kernel
     uint4 *afrag;         // [th][256 * 256 / 4] stage matrix in MMA-fragment order (MIXED, 128 < D <= 256)
+    void *mgl;            // global-matrix engine: [th][D][D] stage matrix (float MIXED, double FP64)
+    void *glxc;           // global-matrix engine: [th][16][D] chain states of the slots (same type)
     int *queue;           // device counter of the persistent launch (nullptr: one CTA per G geometries)
     const double *b;      // [th][D]
     const double *dsd;    // [th]
@@ -43,6 +45,9 @@ struct InnerArgs {
 };
 
 cudaError_t launch_gibbs(const MeshDev &m, const InnerArgs &a, cudaStream_t s);
+// true when a batch of this precision / engine / slip dimension runs on the
+// global-matrix engine (InnerArgs::mgl and ::glxc must then be set)
+bool inner_uses_global(int mixed, int engine, int D);
 cudaError_t launch_inner(const MeshDev &m, const InnerArgs &a, cudaStream_t s, const char **why);
 
 // engine families behind launch_inner, one translation unit each
@@ -56,5 +61,7 @@ cudaError_t launch_inner_mma_wide(const MeshDev &m, const InnerArgs &a, cudaStre
 cudaError_t launch_inner_mma_pair(const MeshDev &m, const InnerArgs &a, cudaStream_t s);              // D <= 128
 cudaError_t launch_inner_mma_streamed(const MeshDev &m, const InnerArgs &a, cudaStream_t s);          // 128 < D <= 256
 cudaError_t launch_inner_tc(const MeshDev &m, const InnerArgs &a, cudaStream_t s);                    // D <= 128
+cudaError_t launch_inner_gl32(const MeshDev &m, const InnerArgs &a, cudaStream_t s);                  // D <= 1024
+cudaError_t launch_inner_gl64(const MeshDev &m, const InnerArgs &a, cudaStream_t s);                  // D <= 512
 
 }  // namespace smc

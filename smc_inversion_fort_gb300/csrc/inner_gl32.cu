@@ -1,0 +1,13 @@
+// Inner SMC, global-matrix engine in MIXED precision (FP32 stage matrix in
+// global memory): D <= 256, 512 and 1024 tiles.
+#include "inner_impl.cuh"
+
+namespace smc {
+
+cudaError_t launch_inner_gl32(const MeshDev &m, const InnerArgs &a, cudaStream_t s) {
+    if (a.D <= 256) return launch_gl_t<float, 16>(m, a, s);
+    if (a.D <= 512) return launch_gl_t<float, 32>(m, a, s);
+    return launch_gl_t<float, 64>(m, a, s);
+}
+
+}  // namespace smc

@@ -68,7 +68,7 @@ constexpr int CW = 8;    // chain slots per warp (CUDA-core engine)
 constexpr int CTW = 4;   // slots per lane
 constexpr int RGW = 16;  // row groups per warp
 constexpr uint32_t WAIT_TRIES = 1u << 22;   // bounded mbarrier wait
-enum : int { ENG_CC = 0, ENG_TC = 1, ENG_MMA = 2 };   // step engines
+enum : int { ENG_CC = 0, ENG_TC = 1, ENG_MMA = 2, ENG_GL = 3 };   // step engines
 
 // ---- warp-level tensor-core MMA (BF16 in, FP32 accumulate), m16n8k16
 __device__ __forceinline__ void ldsm_x4(uint32_t r[4], const void *p) {
@@ -209,6 +209,72 @@ __device__ __forceinline__ double wreduce16(double v[16], int lane) {
         }
     }
     return v[0] + __shfl_xor_sync(FULL, v[0], 1);
+}
+
+// Sum of NV per-slot values over the 32 lanes of a warp: afterwards lane l
+// holds the total of value l / (32 / NV) (NV = 8 or 16).
+template <int NV>
+__device__ __forceinline__ double wreduce_n(double v[NV], int lane) {
+#pragma unroll
+    for (int o = 16, n = NV; n >= 2; o >>= 1, n >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < n / 2; ++i) {
+            double send = up ? v[i] : v[i + n / 2];
+            double keep = up ? v[i + n / 2] : v[i];
+            v[i] = keep + __shfl_xor_sync(FULL, send, o);
+        }
+    }
+    double t = v[0];
+#pragma unroll
+    for (int o = 16 / NV; o >= 1; o >>= 1) t += __shfl_xor_sync(FULL, t, o);
+    return t;
+}
+
+// Global-matrix step product: acc[i][s] = sum_k Mg[k][r_i] X[k][s0 + s] for the
+// thread's rows r_i = row0 + i * RP (column-major Mg with leading dimension
+// D, read through L1/L2 with plain loads: the matrix is rewritten every
+// stage) and its SPT slots of the shared operand X (row stride S).
+template <typename T, int R, int SPT, int RP, int S>
+__device__ __forceinline__ void gl_gemm(const T *Mg, int D, const T *__restrict__ X, int row0, int s0,
+                                        T acc[R][SPT]) {
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+        for (int q = 0; q < SPT; ++q) acc[i][q] = T(0);
+    bool live[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) live[i] = row0 + i * RP < D;
+#pragma unroll 4
+    for (int k = 0; k < D; ++k) {
+        T mv[R];
+#pragma unroll
+        for (int i = 0; i < R; ++i) mv[i] = live[i] ? Mg[(size_t)k * D + row0 + i * RP] : T(0);
+        const T *xk = X + k * S + s0;   // 16-byte aligned: S and s0 are multiples of 8
+        if constexpr (sizeof(T) == 4) {
+#pragma unroll
+            for (int q = 0; q < SPT; q += 4) {
+                const float4 v = *reinterpret_cast<const float4 *>(xk + q);
+#pragma unroll
+                for (int i = 0; i < R; ++i) {
+                    acc[i][q] = fmaf((float)mv[i], v.x, (float)acc[i][q]);
+                    acc[i][q + 1] = fmaf((float)mv[i], v.y, (float)acc[i][q + 1]);
+                    acc[i][q + 2] = fmaf((float)mv[i], v.z, (float)acc[i][q + 2]);
+                    acc[i][q + 3] = fmaf((float)mv[i], v.w, (float)acc[i][q + 3]);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < SPT; q += 2) {
+                const double2 v = *reinterpret_cast<const double2 *>(xk + q);
+#pragma unroll
+                for (int i = 0; i < R; ++i) {
+                    acc[i][q] = fma((double)mv[i], v.x, (double)acc[i][q]);
+                    acc[i][q + 1] = fma((double)mv[i], v.y, (double)acc[i][q + 1]);
+                }
+            }
+        }
+    }
 }
 
 // Group of W warps (W*32 threads) synchronised by named barrier id+1.
@@ -365,7 +431,10 @@ struct Layout {
     // in fragment order and streamed through a per-warp ring, and the FP32 Gram
     // matrix of the end-point energies is read from global memory
     static constexpr bool AGL = ENG == ENG_MMA && DP > 128;
-    static constexpr int S = ENG == ENG_CC ? CW : (AGL ? 4096 / DP : 2048 / DP);   // slots per warp (CC) / group
+    // global-matrix engine: 16 slots per group of 16 warps; a thread owns
+    // GL_SPT slots of one slot group and DP / (512 * GL_SPT / 16) rows
+    static constexpr int GL_SPT = DP <= 256 ? 8 : 16;
+    static constexpr int S = ENG == ENG_CC ? CW : ENG == ENG_GL ? 16 : (AGL ? 4096 / DP : 2048 / DP);   // slots per warp (CC) / group
     static constexpr int RING = 6;                       // streamed k-tiles in flight per warp
     static constexpr uint32_t LBO_A = 2048;              // tcgen05: 128 rows x 16 B per k block
     static constexpr uint32_t LBO_B = 16 * S + 16;       // tcgen05: S rows x 16 B per k block, padded
@@ -382,6 +451,7 @@ struct Layout {
         return AGL ? (size_t)W * RING * mtiles_per_warp(W) * 2 * 32 * 16 : 0;
     }
     __host__ __device__ static size_t engine_bytes(int W) {
+        if (ENG == ENG_GL) return (size_t)DP * S * sizeof(T);  // the step operand [row][slot]
         if (ENG == ENG_TC) return 2 * A_BYTES + 2 * B_BYTES;   // the end-point tile Xf aliases B
         if (ENG == ENG_MMA)   // + the FP32 Gram matrix for the end-point energies (or the A ring)
             return 2 * A_BYTES + 4 * B_BYTES + 3 * TILE_BYTES +
@@ -392,6 +462,9 @@ struct Layout {
     // per-slot partial sums of the end-point energies: 5 x 32 W floats (warp MMA)
     // or 5 x 32 max(W, 4) doubles (tcgen05)
     __host__ __device__ static size_t red_bytes(int W) {
+        if (ENG == ENG_GL)   // per-warp, per-slot partial sums of 5 quantities (also 32 W floats of moments)
+            return (size_t)5 * W * S * sizeof(double) > (size_t)32 * W * sizeof(float)
+                       ? (size_t)5 * W * S * sizeof(double) : (size_t)32 * W * sizeof(float);
         return ENG == ENG_MMA ? (size_t)5 * 32 * W * sizeof(float) : (size_t)5 * 32 * (W > 4 ? W : 4) * sizeof(double);
     }
     __host__ __device__ static size_t bytes(int W) {
@@ -411,7 +484,7 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
     constexpr int DP = L_::DP;
     constexpr bool MIXED = std::is_same<T, float>::value;
     constexpr bool TC = ENG == ENG_TC;
-    static_assert(ENG == ENG_CC || MIXED, "tensor-core engines are MIXED only");
+    static_assert(ENG == ENG_CC || ENG == ENG_GL || MIXED, "tensor-core engines are MIXED only");
     const int lane = grp.lane;
     const int N = a.N, D = a.D, NP2 = a.NP2;
     const int rg = lane & 15, cg = lane >> 4, gt = grp.gt, gnt = grp.nt, wl = grp.wl, W = grp.W;
@@ -432,6 +505,9 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
         if constexpr (L_::AGL) aring = (uint4 *)((unsigned char *)tXC + L_::TILE_BYTES);
         else tA32 = (float *)((unsigned char *)tXC + L_::TILE_BYTES);
         static_assert(2 * L_::B_BYTES >= L_::TILE_BYTES, "offset tile must fit in one B buffer");
+    } else if constexpr (ENG == ENG_GL) {
+        Msm = nullptr;
+        Xw0 = (T *)sp;   // step operand [row][slot]
     } else if constexpr (TC) {
         Ahi = sp; Alo = Ahi + L_::A_BYTES; Bhi = Alo + L_::A_BYTES; Blo = Bhi + L_::B_BYTES;
         Xf = (float *)Bhi;   // written at the last leapfrog step, after the last MMA read B
@@ -644,7 +720,7 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
             }
             grp.sync();
         }
-        if constexpr (MIXED && ENG != ENG_CC) {
+        if constexpr (MIXED && ENG != ENG_CC && ENG != ENG_GL) {
             // thread (d, kp) sums particles k = kp, kp + KP, ...; partials in FP32
             const int KP = gnt / DP, d = gt % DP, kp = gt / DP;
             float *fs = (float *)red;
@@ -773,6 +849,24 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                     tc::split_bf16(v, rh[k], rl[k]);
                 }
             }
+        } else if constexpr (ENG == ENG_GL) {
+            // M = gamma A + L^T L / alpha^2 in global memory, column-major, in T
+            // (MIXED: from the FP32 copy of A, as the warp-MMA engine)
+            T *Mw = (T *)a.mgl + (size_t)th * D * D;
+            if constexpr (MIXED) {
+                const float gf = (float)gamma;
+                for (int e = gt; e < D * D; e += gnt) Mw[e] = gf * A32[e];
+            } else {
+                for (int e = gt; e < D * D; e += gnt) Mw[e] = (T)(gamma * Ath[e]);
+            }
+            grp.sync();
+            const float ia2 = (float)(1.0 / alpha2);
+            for (int i = gt; i < D; i += gnt)
+                for (int e = m.ll_ptr[i]; e < m.ll_ptr[i + 1]; ++e) {
+                    const int k = m.ll_col[e];
+                    if constexpr (MIXED) Mw[(size_t)k * D + i] += (float)llv[e] * ia2;
+                    else Mw[(size_t)k * D + i] = (T)((double)Mw[(size_t)k * D + i] + llv[e] / alpha2);
+                }
         } else if constexpr (TC) {
             // row t of the 128-row A operand is M's row t % DP, split into BF16 hi + lo
             const int i = gt % DP;
@@ -1308,6 +1402,312 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                             const int c = e / DP, r = e % DP;
                             if (r < D && ((actm >> c) & 1ull)) pnew[(size_t)sj[c] * D + r] = (double)tXC[r * TS + c];
                         }
+                }
+                grp.sync();
+            } else if constexpr (ENG == ENG_GL) {
+                // ================= global-matrix engine (any D up to DP): S = 16
+                // slots per group of WG warps.  The stage matrix M (D x D,
+                // column-major, T) is in global memory and each step streams it
+                // once; the slots' operand (MIXED: offsets x - sbar; FP64: x) is a
+                // [row][slot] tile in shared memory.  Thread (sg, t') owns slots
+                // sg * SPT .. + SPT - 1 and rows t', t' + RP, ... (R rows): its
+                // positions and momenta stay in registers for the trajectory.
+                // Chain states (the last accepted positions) are kept per slot
+                // in global memory (InnerArgs::glxc).
+                constexpr int S = L_::S, SPT = L_::GL_SPT, SG = S / SPT, NTH = 32 * WG, RP = NTH / SG;
+                constexpr int R = DP / RP, WPG = RP / 32;   // rows per thread, warps per slot group
+                static_assert(R * RP == DP && SG * SPT == S && S <= 32, "global-matrix engine tiling");
+                const int sg = gt / RP, row0 = gt % RP, s0 = sg * SPT;
+                T *Xs = Xw0;
+                unsigned *m32 = (unsigned *)masks;   // [0] fresh [2] active [4] blown [6] accepted
+                const T *Mg = (const T *)a.mgl + (size_t)th * D * D;
+                T *xct = (T *)a.glxc + (size_t)th * S * D;
+                T cov_r[R], mean_r[R], cv_r[R], isc_r[R];
+                double vcov_r[R];
+                bool live_r[R];
+#pragma unroll
+                for (int i = 0; i < R; ++i) {
+                    const int r = row0 + i * RP;
+                    live_r[i] = r < D;
+                    cov_r[i] = tcov[r];
+                    mean_r[i] = tmean[r];
+                    cv_r[i] = tcv[r];
+                    isc_r[i] = tisc[r];
+                    vcov_r[i] = vcov[r];
+                }
+                double *redd = red;   // [q][warp][slot in group]
+                if (gt == 0) gint[0] = 0;
+                if (gt < 8) m32[gt] = 0u;
+                if (gt < S) { sj[gt] = 0; sjend[gt] = 0; spar[gt] = -1; }
+                // operand tile from the thread's rows (MIXED: offsets from the stage mean)
+                auto write_x = [&](const T (&xx)[R][SPT], unsigned actm) {
+#pragma unroll
+                    for (int i = 0; i < R; ++i) {
+                        const int r = row0 + i * RP;
+                        T v[SPT];
+#pragma unroll
+                        for (int q = 0; q < SPT; ++q) {
+                            const bool on = live_r[i] && ((actm >> (s0 + q)) & 1u);
+                            v[q] = on ? (MIXED ? xx[i][q] - mean_r[i] : xx[i][q]) : T(0);
+                        }
+                        if constexpr (sizeof(T) == 4) {
+#pragma unroll
+                            for (int q = 0; q < SPT; q += 4)
+                                *reinterpret_cast<float4 *>(Xs + r * S + s0 + q) =
+                                    make_float4((float)v[q], (float)v[q + 1], (float)v[q + 2], (float)v[q + 3]);
+                        } else {
+#pragma unroll
+                            for (int q = 0; q < SPT; q += 2)
+                                *reinterpret_cast<double2 *>(Xs + r * S + s0 + q) = make_double2(v[q], v[q + 1]);
+                        }
+                    }
+                };
+                while (true) {
+                    grp.sync();
+                    // slot refill: thread c < S advances its chain or takes the next parent
+                    if (gt < 32) {
+                        const int c = gt;
+                        bool fresh = false, act = false;
+                        if (c < S) {
+                            if ((m32[2] >> c) & 1u) sj[c] += 1;
+                            if (sj[c] >= sjend[c]) {
+                                const int qi = atomicAdd(&gint[0], 1);
+                                if (qi < nq) {
+                                    const int k = keys[qi] & 0xffff;
+                                    spar[c] = k;
+                                    sj[c] = ids[k];
+                                    sjend[c] = ids[k] + cnt[k];
+                                    fresh = true;
+                                    sL[c] = Lc[k];
+                                    sP[c] = Pc[k];
+                                    spost[c] = gamma * Lc[k] + Pc[k];
+                                }
+                            }
+                            act = sj[c] < sjend[c];
+                            sdt[c] = act ? dtau[sj[c]] : 0.0;
+                        }
+                        const unsigned fm = __ballot_sync(FULL, fresh), am = __ballot_sync(FULL, act);
+                        if (lane == 0) { m32[0] = fm; m32[2] = am; m32[4] = 0u; }
+                    }
+                    grp.sync();
+                    const unsigned actm = m32[2], frm = m32[0];
+                    if (actm == 0u) break;
+                    // chain start: a fresh slot's chain state is its parent
+                    if (frm != 0u) {
+                        for (int e = gt; e < S * D; e += NTH) {
+                            const int c = e / D, r = e % D;
+                            if ((frm >> c) & 1u) xct[e] = (T)parts[(size_t)spar[c] * D + r];
+                        }
+                        grp.sync();
+                    }
+                    // per-slot sums over the thread's rows, reduced over each warp into
+                    // redd[q][warp][slot]: q = 0 likelihood, 1 prior, 2 end kinetic
+                    // energy, 3 tuning distance, 4 start kinetic energy
+                    auto put = [&](double (&v)[SPT], int qq) {
+                        const double t = wreduce_n<SPT>(v, lane);
+                        if ((lane % (32 / SPT)) == 0) redd[(qq * WG + wl) * SPT + lane / (32 / SPT)] = t;
+                    };
+                    T x[R][SPT], p[R][SPT], dts[SPT];
+                    double kin[SPT];
+#pragma unroll
+                    for (int q = 0; q < SPT; ++q) {
+                        const int c = s0 + q;
+                        const bool on = (actm >> c) & 1u;
+                        const int jj = sj[c];
+                        dts[q] = (T)sdt[c];
+                        kin[q] = 0.0;
+#pragma unroll
+                        for (int i = 0; i < R; ++i) {
+                            const int r = row0 + i * RP;
+                            T xv = T(0), pv = T(0);
+                            if (on && live_r[i]) {
+                                xv = xct[(size_t)c * D + r];
+                                if constexpr (MIXED) {
+                                    const float2 z = rng_normal2_f(a.seed, stream, P_MOM, iter, jj, (uint64_t)(r >> 1));
+                                    pv = ((r & 1) ? z.y : z.x) * isc_r[i];
+                                    kin[q] += (double)(pv * cov_r[i] * pv * 0.5f);
+                                } else {
+                                    pv = (T)(rng_normal(a.seed, stream, P_MOM, iter, jj, r) / sqrt(vcov_r[i]));
+                                    kin[q] += (double)pv * vcov_r[i] * (double)pv / 2.0;
+                                }
+                            }
+                            x[i][q] = xv;
+                            p[i][q] = pv;
+                        }
+                    }
+                    put(kin, 4);
+                    // leapfrog (smc_slip.f90:755-904): P/2 (X P)^ntau X/2
+                    int flag = 0;
+                    const float imx = 1.0f / (float)mx;
+                    for (int it = 0; it <= a.ntau; ++it) {
+                        write_x(x, actm);
+                        grp.sync();
+                        T acc[R][SPT];
+                        gl_gemm<T, R, SPT, RP, S>(Mg, D, Xs, row0, s0, acc);
+                        grp.sync();
+                        const unsigned blm = m32[4];
+                        const T hs = it == 0 ? T(0.5) : T(1), xs = it == a.ntau ? T(0.5) : T(1);
+#pragma unroll
+                        for (int q = 0; q < SPT; ++q) {
+                            const int c = s0 + q;
+                            const bool on = ((actm >> c) & 1u) && !((blm >> c) & 1u);
+#pragma unroll
+                            for (int i = 0; i < R; ++i) {
+                                if (!(on && live_r[i])) continue;
+                                const T gr = MIXED ? cv_r[i] + acc[i][q] : acc[i][q] - cv_r[i];
+                                p[i][q] = p[i][q] - gr * hs * dts[q];
+                                x[i][q] = x[i][q] + cov_r[i] * p[i][q] * xs * dts[q];
+                                if constexpr (MIXED) {
+                                    const bool blow = (x[i][q] < T(0) ? -x[i][q] : x[i][q]) > T(1e3);
+                                    if (blow) atomicOr(&m32[4], 1u << c);
+                                    else reflect_fold(x[i][q], p[i][q], mx, imx);
+                                } else if (blow_or_reflect<T>(x[i][q], p[i][q], mx, flag)) {
+                                    atomicOr(&m32[4], 1u << c);
+                                }
+                            }
+                        }
+                    }
+                    status |= flag;
+                    // end point: the operand (offsets, or positions in FP64) and A times it
+                    write_x(x, actm);
+                    grp.sync();
+                    const unsigned blm = m32[4];
+                    T af[R][SPT];
+                    if constexpr (MIXED) gl_gemm<T, R, SPT, RP, S>((const T *)A32, D, Xs, row0, s0, af);
+                    else gl_gemm<T, R, SPT, RP, S>((const T *)Ath, D, Xs, row0, s0, af);
+                    // per-slot sums over the thread's rows, one quantity at a time
+                    double v[SPT];
+                    // likelihood term (MIXED: g.delta + delta.A delta / 2; FP64: x.A x - 2 b.x)
+#pragma unroll
+                    for (int q = 0; q < SPT; ++q) {
+                        v[q] = 0.0;
+                        if (!((actm >> (s0 + q)) & 1u)) continue;
+#pragma unroll
+                        for (int i = 0; i < R; ++i) {
+                            if (!live_r[i]) continue;
+                            const int r = row0 + i * RP;
+                            if constexpr (MIXED) {
+                                const float dr = x[i][q] - mean_r[i];
+                                v[q] += (double)((float)tvg[r] * dr + 0.5f * dr * af[i][q]);
+                            } else {
+                                const double xv = (double)x[i][q];
+                                v[q] += xv * (double)af[i][q] - 2.0 * vb[r] * xv;
+                            }
+                        }
+                    }
+                    put(v, 0);
+                    // prior term (MIXED: h.delta + |L delta|^2 / (2 alpha^2); FP64: |L x|^2 / (2 alpha^2))
+#pragma unroll
+                    for (int q = 0; q < SPT; ++q) {
+                        v[q] = 0.0;
+                        if constexpr (MIXED) {
+                            if (!((actm >> (s0 + q)) & 1u)) continue;
+#pragma unroll
+                            for (int i = 0; i < R; ++i)
+                                if (live_r[i]) v[q] += (double)((float)tvh[row0 + i * RP] * (x[i][q] - mean_r[i]));
+                        }
+                    }
+                    for (int r2 = row0; r2 < m.nrow; r2 += RP) {
+#pragma unroll
+                        for (int q = 0; q < SPT; ++q) {
+                            const int c = s0 + q;
+                            if (!((actm >> c) & 1u)) continue;
+                            double t = 0.0;
+                            for (int k9 = 0; k9 < 9; ++k9) {
+                                const int cl = m.l_col[r2 * 9 + k9];
+                                if (cl >= 0) t += lv[(size_t)r2 * 9 + k9] * (double)Xs[cl * S + c];
+                            }
+                            v[q] += t * t / (2.0 * alpha2);
+                        }
+                    }
+                    put(v, 1);
+                    // end kinetic energy
+#pragma unroll
+                    for (int q = 0; q < SPT; ++q) {
+                        v[q] = 0.0;
+                        if (!((actm >> (s0 + q)) & 1u)) continue;
+#pragma unroll
+                        for (int i = 0; i < R; ++i) {
+                            if (!live_r[i]) continue;
+                            if constexpr (MIXED) v[q] += (double)(0.5f * p[i][q] * cov_r[i] * p[i][q]);
+                            else v[q] += (double)p[i][q] * vcov_r[i] * (double)p[i][q] / 2.0;
+                        }
+                    }
+                    put(v, 2);
+                    // tuning distance from the chain start
+#pragma unroll
+                    for (int q = 0; q < SPT; ++q) {
+                        v[q] = 0.0;
+                        const int c = s0 + q;
+                        if (!((actm >> c) & 1u)) continue;
+#pragma unroll
+                        for (int i = 0; i < R; ++i) {
+                            if (!live_r[i]) continue;
+                            const int r = row0 + i * RP;
+                            const T xcv = xct[(size_t)c * D + r];
+                            if constexpr (MIXED) {
+                                const float dx = x[i][q] - xcv;
+                                v[q] += (double)(dx * dx * (float)ticov[r]);
+                            } else {
+                                const double dx = (double)x[i][q] - (double)xcv;
+                                v[q] += dx * dx / vcov_r[i];
+                            }
+                        }
+                    }
+                    put(v, 3);
+                    grp.sync();
+                    // Metropolis test and bookkeeping (smc_slip.f90:695-716, 1057-1094)
+                    if (gt < 32) {
+                        const int c = gt;
+                        bool accd = false;
+                        if (c < S && ((actm >> c) & 1u)) {
+                            const int g0 = (c / SPT) * WPG, cq = c % SPT;
+                            double q5[5];
+#pragma unroll
+                            for (int qq = 0; qq < 5; ++qq) {
+                                double t = 0.0;
+                                for (int w2 = 0; w2 < WPG; ++w2) t += redd[(qq * WG + g0 + w2) * SPT + cq];
+                                q5[qq] = t;
+                            }
+                            const int jj = sj[c];
+                            const bool blown = (blm >> c) & 1u;
+                            const double Lx = MIXED ? q5[0] + Lbar : (q5[0] + dsd) / 2.0 + lconst;
+                            const double Px = MIXED ? q5[1] + Pbar : q5[1];
+                            const double post = gamma * Lx + Px;
+                            const double ham = blown ? 1e20 : post + q5[2];
+                            const double dham = (spost[c] + q5[4]) - ham;
+                            if (tuning) score[jj] = blown ? 0.0 : q5[3] * exp(fmin(0.0, dham));
+                            const double u = rng_uniform(a.seed, stream, P_MH, iter, jj, 0);
+                            if (!blown && dham > log(u)) {
+                                accd = true;
+                                sL[c] = Lx;
+                                sP[c] = Px;
+                                spost[c] = post;
+                            }
+                            if (!tuning) {
+                                Ln[jj] = sL[c];
+                                Pn[jj] = sP[c];
+                            }
+                        }
+                        const unsigned am = __ballot_sync(FULL, accd);
+                        if (lane == 0) m32[6] = am;
+                    }
+                    grp.sync();
+                    const unsigned accm = m32[6];
+#pragma unroll
+                    for (int q = 0; q < SPT; ++q) {
+                        const int c = s0 + q;
+                        if (!((actm >> c) & 1u)) continue;
+                        const bool accd = (accm >> c) & 1u;
+#pragma unroll
+                        for (int i = 0; i < R; ++i) {
+                            if (!live_r[i]) continue;
+                            const int r = row0 + i * RP;
+                            T *xp = xct + (size_t)c * D + r;
+                            if (accd) *xp = x[i][q];
+                            if (!tuning) pnew[(size_t)sj[c] * D + r] = (double)(accd ? x[i][q] : *xp);
+                        }
+                    }
                 }
                 grp.sync();
             } else if constexpr (TC) {
@@ -1852,7 +2252,7 @@ __host__ __device__ constexpr uint32_t tmem_columns(int n) {
 }
 
 template <typename T, int RT, int ENG, int WG>
-__global__ void __launch_bounds__(ENG == ENG_MMA ? 512 : 256) inner_group_kernel(MeshDev m, InnerArgs a, int W, int G) {
+__device__ __forceinline__ void inner_group_entry(const MeshDev &m, const InnerArgs &a, int W, int G) {
     extern __shared__ __align__(128) unsigned char smem_all[];
     __shared__ uint32_t tmem_slot;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1904,6 +2304,18 @@ __global__ void __launch_bounds__(ENG == ENG_MMA ? 512 : 256) inner_group_kernel
         tc::fence_after_sync();
         if (warp == 0) tc::tmem_dealloc(tmem_base, ncols);
     }
+}
+
+template <typename T, int RT, int ENG, int WG>
+__global__ void __launch_bounds__(ENG == ENG_MMA ? 512 : 256) inner_group_kernel(MeshDev m, InnerArgs a, int W, int G) {
+    inner_group_entry<T, RT, ENG, WG>(m, a, W, G);
+}
+
+// the global-matrix engine: one 512-thread CTA per SM, so up to 128 registers
+// per thread for the positions, momenta and products of its rows and slots
+template <typename T, int RT>
+__global__ void __launch_bounds__(512, 1) inner_gl_kernel(MeshDev m, InnerArgs a) {
+    inner_group_entry<T, RT, ENG_GL, 16>(m, a, 16, 1);
 }
 
 // CTAs of a persistent launch: one wave (resident CTAs), no more than the
@@ -1977,6 +2389,30 @@ static cudaError_t launch_wg_t(const MeshDev &m, const InnerArgs &a, cudaStream_
         if (!blocks) return cudaGetLastError();
     }
     inner_group_kernel<float, RT, ENG, WG><<<blocks, 32 * WG * G, sm, s>>>(m, a, WG, G);
+    return cudaGetLastError();
+}
+
+// Global-matrix engine: one geometry per CTA of 16 warps, persistent over the
+// batch (a CTA takes the next geometry from the queue when it finishes one).
+template <typename T, int RT>
+static cudaError_t launch_gl_t(const MeshDev &m, const InnerArgs &a, cudaStream_t s) {
+    using L_ = Layout<T, RT, ENG_GL>;
+    constexpr int WG = 16;
+    if (a.D > L_::DP || !a.mgl || !a.glxc || !a.queue) return cudaErrorInvalidValue;
+    if (!std::is_same<T, double>::value && !a.A32) return cudaErrorInvalidValue;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const size_t sm = L_::bytes(WG);
+    cudaError_t e = cudaFuncSetAttribute(inner_gl_kernel<T, RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, inner_gl_kernel<T, RT>, 32 * WG, sm);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) return cudaErrorInvalidConfiguration;
+    const unsigned blocks = persistent_blocks(a, 1, nsm * occ, s);
+    if (!blocks) return cudaGetLastError();
+    inner_gl_kernel<T, RT><<<blocks, 32 * WG, sm, s>>>(m, a);
     return cudaGetLastError();
 }
 

@@ -1,10 +1,10 @@
-"""Nested likelihood above 128 slip dimensions (MIXED only).
+"""Nested likelihood above 128 slip dimensions, warp-MMA engine (MIXED).
 
 Beyond 128 dimensions the stage matrix of the inner HMC step no longer fits in
 shared memory; the warp-MMA engine then streams it from global memory in
-fragment order.  There is no FP64 GPU path at these sizes, so the MIXED
-results are checked against the FP64 oracle (D = 256) and against the
-independent FP32 CUDA-core engine (D = 160), statistically over independent
+fragment order.  Its results are checked against the FP64 oracle (D = 256)
+and against the independent FP32 CUDA-core engine (D = 160), statistically
+over independent
 streams: the mean and the median -log Z agree within 4 standard errors (the
 median of n draws has standard error about 1.2533 sd / sqrt(n)).
 """
@@ -89,12 +89,3 @@ def test_d256_posterior_mean_matches_oracle(smcgpu, orc):
     diff = np.abs(mg.mean(0) - mr.mean(0))
     print("max |diff|", diff.max(), "max se", se.max())
     assert np.all(diff < 4 * se + 0.02 * true_slip(w).max())
-
-
-def test_fp64_above_128_dimensions_is_an_error(smcgpu, orc):
-    """The FP64 inner kernel stops at 128 slip dimensions: a clear error, no fallback."""
-    w, obs, o = setup_case("d160", orc)
-    g = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
-    g.set_data(obs)
-    with pytest.raises(Exception, match="D <= 128"):
-        g.fault_calc_likelihood(true_theta(w)[None], 1, np.zeros(1, np.uint64))
