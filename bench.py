@@ -42,11 +42,13 @@ def parse():
     p.add_argument("--n-theta", type=int, default=8192)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-nested", action="store_true")
-    p.add_argument("--no-c2", action="store_true", help="skip the c2 (D = 256) nested sample")
-    p.add_argument("--c2-cpu-baseline", action="store_true",
-                   help="also time the oracle on c2 (16 geometries, one per host thread: about 2.5 minutes, the "
-                        "slowest geometry sets the wall time)")
-    p.add_argument("--outer-stages", type=int, default=1)
+    p.add_argument("--no-c2", action="store_true", help="skip the c2 (D = 256) nested measurements")
+    p.add_argument("--no-c4", action="store_true", help="skip the c4 (D = 1024) nested sample")
+    p.add_argument("--fp64-stages", type=int, default=3, help="c0 outer stages timed in FP64")
+    p.add_argument("--equal-error-study", type=str, default=None, metavar="OUT_JSON",
+                   help="instead of the benchmark: full c0 outer-SMC runs over several seeds in MIXED and FP64 "
+                        "(posterior mean / std of every geometry parameter and the evidence), written to OUT_JSON")
+    p.add_argument("--study-seeds", type=str, default="8,3", help="MIXED,FP64 seeds of the equal-error study")
     return p.parse_args()
 
 
@@ -63,8 +65,16 @@ def workload(n_theta):
     return w, obs, th
 
 
+def c1_config(n_theta, nobs, D):
+    return {"workload": "c1: 8192 geometries x 16x8 patches x 5x5 Gauss points x 400 stations (3-comp), "
+                        "patch-constant basis, FP64",
+            "n_theta": n_theta, "nobs": nobs, "D": D, "entries_per_step": n_theta * nobs * D,
+            "l2": "output 20.1 GB per step, larger than L2; no flush needed"}
+
+
 def cpu_greens_rate(w, obs, th, target_s=15.0, max_theta=512):
-    """Oracle Green's build on all host threads over a bounded sample."""
+    """Oracle (timing build) Green's build on all host threads over a bounded
+    sample of the geometries; returns the rate and the sample's wall time."""
     from oracle import pyoracle
     pyoracle.build()
     o = pyoracle.Oracle(w.settings, obs)
@@ -79,30 +89,38 @@ def cpu_greens_rate(w, obs, th, target_s=15.0, max_theta=512):
     dt = time.perf_counter() - t0
     D, nobs = o.dims["D"], o.nobs
     return {"value": n * nobs * D / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{n} of {len(th)} geometries, full 1200x256 matrices, {dt:.1f} s wall"}
+            "sample": f"{n} of {len(th)} geometries, full 1200x256 matrices, {dt:.1f} s wall (oracle timing "
+                      f"build, -O3)", "wall_s": dt}
 
 
 def reference_arm(args):
+    """The CPU restatement of the reference path (oracle/, -O3 timing build)
+    on every host thread: a step is a bounded sample of the c1 workload (the
+    same geometries as the GPU arm's step), its value the sample's entries
+    over its wall time."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    from oracle import pyoracle
+    pyoracle.use_timing_build()
     w, obs, th = workload(args.n_theta)
-    vals = []
+    vals, walls = [], []
     cb = None
     for k in range(args.warmup + args.steps):
         r = cpu_greens_rate(w, obs, th, target_s=8.0 if k >= args.warmup else 2.0, max_theta=256)
         if k >= args.warmup:
             vals.append(r["value"])
+            walls.append(r["wall_s"])
             cb = r
     v = statistics.median(vals)
     D = w.settings.dims()["D"]
     nobs = 3 * 400
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": args.n_theta * nobs * D / v * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": "c1: 8192 geometries x 16x8 patches x 5x5 Gauss points x 400 stations (3-comp)",
-                       "n_theta": args.n_theta, "nobs": nobs, "D": D},
+            "warmup": args.warmup, "ms_per_step": statistics.mean(walls) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded stations, prior-box "
+            "geometries)", "impl": "reference",
+            "config": c1_config(args.n_theta, nobs, D),
+            "step": "a bounded sample of the workload's geometries per step (ms_per_step is its measured wall time)",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": "port", "sample": cb["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -173,120 +191,243 @@ def load_traffic():
     return None
 
 
-def nested_workload(seed=2024):
-    """c0: 8x4 patches x 2 components (D = 64), 60 three-component GNSS
-    stations, 500 inner and 500 outer particles; data from the known fault."""
+def nested_workload(pkg, name="c0", seed=2024):
+    """Seeded observations of a named workload, data from its known fault
+    (the GPU Green's build of the true geometry plus Gaussian noise)."""
     from smc_inversion_fort_gb300.configs import make_stations, preset, prior_range, true_slip, true_theta
-    w = preset("c0")
+    w = preset(name)
     rng = np.random.default_rng(seed)
     obs = make_stations(w, rng)
-    return w, obs, rng, prior_range(w), true_theta(w), true_slip(w)
-
-
-def nested_bench(pkg, torch, stages=1, cpu=True):
-    """Outer particles/s of the nested SMC on c0, FP64 and MIXED, and the
-    MIXED-vs-FP64 evidence difference."""
-    import dataclasses
-    w, obs, rng, rg, th_true, s_true = nested_workload()
     obs["dvec"] = np.zeros(len(obs["obs_sigma"]))
     g = pkg.SmcGpu(w.settings)
     g.set_data(obs)
-    G = g.calc_greens_func(th_true[None])[0]
-    obs["dvec"] = G.T @ s_true + rng.standard_normal(G.shape[1]) * obs["obs_sigma"]
+    G = g.calc_greens_func(true_theta(w)[None])[0]
+    g.close()
+    obs["dvec"] = G.T @ true_slip(w) + rng.standard_normal(G.shape[1]) * obs["obs_sigma"]
+    return w, obs, prior_range(w), true_theta(w), true_slip(w)
+
+
+def inner_roofline(st, ntau, D, peak, peak_name):
+    """Algorithmic flops of the inner SMC kernel over a run: every HMC
+    trajectory (tuning and sampling) takes ntau + 1 Gram-matrix products
+    M x (2 D^2 each) and one A x for its end-point energy (2 D^2), the Gram
+    form of slip_calc_grad / slip_calc_likelihood (smc_slip.f90:56-182)."""
+    flops = st["inner_trajectories"] * (ntau + 2) * 2.0 * D * D
+    ach = flops / (st["inner_kernel_ms"] * 1e-3) / 1e12 if st["inner_kernel_ms"] > 0 else 0.0
+    return {"bound": "tensor" if "bf16" in peak_name else "fp64", "achieved": ach, "peak": peak,
+            "unit": "TFLOP/s", "frac": ach / peak if peak else None, "peak_source": peak_name,
+            "flops_per_trajectory": (ntau + 2) * 2 * D * D, "trajectories": st["inner_trajectories"],
+            "inner_kernel_s": st["inner_kernel_ms"] * 1e-3, "inner_share_of_nested_batches":
+                st["inner_kernel_ms"] / st["nested_ms"] if st["nested_ms"] else None,
+            "mean_inner_stages": st["inner_stages"] / max(st["nested_evals"], 1)}
+
+
+def timed_outer_run(pkg, w, obs, rg, prec, seed, max_stages=0):
+    """fault_smc_exec with every stage timed (host wall clock around each
+    stage's device batches) and the run statistics on."""
+    import dataclasses
+    s = dataclasses.replace(w.settings, max_outer_stages=max_stages)
+    g = pkg.SmcGpu(s, prec)
+    g.set_data(obs)
+    g.stats_reset(True)
+    parts, lik, ev, ns = g.fault_smc_exec(rg, w.n_outer, seed)
+    st = g.stats()
+    sec, evs = g.outer_stage_times()
+    g.close()
+    return {"parts": parts, "evidence": ev, "nstage": ns, "stats": st, "stage_s": sec[1:], "stage_evals": evs[1:],
+            "init_s": float(sec[0])}
+
+
+def nested_bench(pkg, torch, peaks, fp64_peak, cpu=True, fp64_stages=3):
+    """Nested SMC on c0 (one rectangle, 8x4 patches x 2 components = 64 slip
+    parameters, 60 GNSS stations, 500 outer x 500 inner particles, ntau 50):
+    outer particles/s averaged over every stage of a full MIXED run; FP64 on
+    its first stages (a full FP64 run is about 13 minutes); MIXED vs FP64 on
+    the same stages; the inner kernel's roofline; the equal-error checks."""
+    w, obs, rg, th_true, s_true = nested_workload(pkg, "c0")
+    N, D, ntau = w.n_outer, w.settings.dims()["D"], w.settings.ntau
     out = {"workload": "c0: 8x4 patches (D=64), 60 GNSS stations (180 obs), 500 inner x 500 outer particles, "
-                       "ntau 50, CV 2 / 0.2", "n_outer": w.n_outer, "timed_outer_stages": stages}
-    for name, prec in (("mixed", pkg.PREC_MIXED), ("fp64", pkg.PREC_FP64)):
-        times = {}
-        for k in (-1, stages):
-            s2 = dataclasses.replace(w.settings, max_outer_stages=k)
-            gg = pkg.SmcGpu(s2, prec)
-            gg.set_data(obs)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            _, _, ev, ns = gg.fault_smc_exec(rg, w.n_outer, 17)
-            torch.cuda.synchronize()
-            times[k] = time.perf_counter() - t0
-            gg.close()
-        per_stage = (times[stages] - times[-1]) / stages
-        out[name] = {"outer_particles_per_s": w.n_outer / per_stage, "s_per_outer_stage": per_stage,
-                     "nested_evals_per_s": 2 * w.n_outer / per_stage, "init_eval_s": times[-1]}
-    # evidence agreement on the true geometry over independent streams
-    # (1024 per precision: standard error about 0.03 nat)
-    reps = 1024
-    thr = np.repeat(th_true[None], reps, 0)
-    st = np.arange(reps, dtype=np.uint64)
-    res = {}
-    for name, prec in (("mixed", pkg.PREC_MIXED), ("fp64", pkg.PREC_FP64)):
-        gg = pkg.SmcGpu(w.settings, prec)
-        gg.set_data(obs)
-        res[name], _ = gg.fault_calc_likelihood(thr, 99, st + (0 if name == "fp64" else 10**6))
-        gg.close()
-    d = res["mixed"].mean() - res["fp64"].mean()
-    se = float(np.sqrt((res["mixed"].var(ddof=1) + res["fp64"].var(ddof=1)) / reps))
-    out["mixed_vs_fp64"] = {"delta_neglog_evidence": float(d), "standard_error": se, "reps": reps,
-                            "fp64_mean": float(res["fp64"].mean()), "fp64_std": float(res["fp64"].std())}
-    out["mixed_speedup_vs_fp64"] = out["mixed"]["outer_particles_per_s"] / out["fp64"]["outer_particles_per_s"]
+                       "ntau 50, CV 2 / 0.2", "n_outer": N}
+    runs = {}
+    for name, prec, k in (("mixed", pkg.PREC_MIXED, 0), ("fp64", pkg.PREC_FP64, fp64_stages)):
+        r = timed_outer_run(pkg, w, obs, rg, prec, 17, k)
+        runs[name] = r
+        ss = r["stage_s"]
+        peak = peaks.get("bf16_tflops_sustained", 1700.0) if name == "mixed" else fp64_peak
+        pname = "bf16_tflops_sustained (MEASURED_PEAKS.json)" if name == "mixed" else "cuBLAS DGEMM in this run"
+        out[name] = {"outer_stages_timed": len(ss), "outer_stages_total": r["nstage"] if k == 0 else None,
+                     "outer_particles_per_s": N * len(ss) / ss.sum(),
+                     "s_per_outer_stage_mean": float(ss.mean()),
+                     "per_stage_outer_particles_per_s": [round(N / x, 1) for x in ss],
+                     "nested_evals_per_s": float(r["stage_evals"].sum() / ss.sum()),
+                     "init_eval_s": r["init_s"], "evidence": r["evidence"] if k == 0 else None,
+                     "roofline_inner": inner_roofline(r["stats"], ntau, D, peak, pname)}
+    k = len(runs["fp64"]["stage_s"])
+    same = runs["mixed"]["stage_s"][:k].sum()
+    out["mixed_speedup_vs_fp64"] = {"same_stages": float(runs["fp64"]["stage_s"].sum() / same), "stages": k,
+                                    "mixed_all_stages_vs_fp64_first_stages":
+                                        out["mixed"]["outer_particles_per_s"] / out["fp64"]["outer_particles_per_s"]}
+    out["mixed_vs_fp64"] = equal_error_c0(pkg, w, obs, rg, th_true)
+    out["mixed_vs_fp64"]["outer_posterior"] = ("full outer-SMC runs over several seeds in both precisions take "
+                                               "about 13 minutes per FP64 run: bench.py --equal-error-study, "
+                                               "summarised in profiles/equal_error_c0.md")
     if cpu:
         out["cpu_baseline"] = cpu_nested_rate(w, obs, rg)
         out["mixed_speedup_vs_cpu"] = out["mixed"]["outer_particles_per_s"] / out["cpu_baseline"]["value"]
     return out
 
 
-def nested_c2_bench(pkg, torch, cpu=True):
-    """Nested evaluations/s on c2 (16x8 patches x 2 components, D = 256; 400
-    GNSS stations and 2000 InSAR points in two paths with a 5 km exponential
-    covariance, 3200 observations; 2048 inner particles, ntau 50), MIXED.
-    Sample: four waves of prior geometries (the inner kernel runs one geometry
-    per CTA at this size, so CTAs that finish early take the next geometries;
-    one wave would time only the slowest geometry), after a small warm-up batch."""
-    from smc_inversion_fort_gb300.configs import make_stations, preset, random_thetas, true_slip, true_theta
-    w = preset("c2")
-    rng = np.random.default_rng(2024)
-    obs = make_stations(w, rng)
-    obs["dvec"] = np.zeros(len(obs["obs_sigma"]))
+def equal_error_c0(pkg, w, obs, rg, th_true, reps=64, n_prior=16):
+    """MIXED against FP64 at equal work: -log Z at the true geometry and at
+    n_prior prior-box geometries (reps independent streams each), and the
+    inner slip posterior (mean and std of every slip component of the final
+    population) at the true geometry over 16 streams."""
+    rng = np.random.default_rng(77)
+    ths = np.vstack([th_true[None], rg[:, 0] + rng.uniform(0, 1, (n_prior, len(rg))) * (rg[:, 1] - rg[:, 0])])
+    thr = np.repeat(ths, reps, axis=0)
+    st = np.arange(len(thr), dtype=np.uint64)
+    res = {}
+    for name, prec in (("mixed", pkg.PREC_MIXED), ("fp64", pkg.PREC_FP64)):
+        g = pkg.SmcGpu(w.settings, prec)
+        g.set_data(obs)
+        v, s = g.fault_calc_likelihood(thr, 99, st + (0 if name == "fp64" else 10**6))
+        res[name] = (v.reshape(len(ths), reps), s)
+        g.close()
+    a, b = res["mixed"][0], res["fp64"][0]
+    d = a.mean(1) - b.mean(1)
+    se = np.sqrt((a.var(1, ddof=1) + b.var(1, ddof=1)) / reps)
+    ev = {"geometries": len(ths), "reps_per_geometry": reps, "delta_neglog_evidence": [round(float(x), 4) for x in d],
+          "standard_error": [round(float(x), 4) for x in se], "fp64_mean": [round(float(x), 3) for x in b.mean(1)],
+          "max_abs_delta": float(np.abs(d).max()), "max_abs_delta_over_se": float((np.abs(d) / se).max()),
+          "within_0p1_nat": int((np.abs(d) <= 0.1).sum()),
+          "within_0p1_nat_or_2se": int((np.abs(d) <= np.maximum(0.1, 2 * se)).sum()),
+          "status_max": int(max(res["mixed"][1].max(), res["fp64"][1].max())),
+          "note": "entry 0 is the true geometry, the others prior-box draws"}
+    # inner slip posterior at the true geometry
+    post = {}
+    for name, prec in (("mixed", pkg.PREC_MIXED), ("fp64", pkg.PREC_FP64)):
+        g = pkg.SmcGpu(w.settings, prec)
+        g.set_data(obs)
+        ms, ss = [], []
+        for k in range(16):
+            p = g.fault_likelihood_posterior(th_true, 123, k + (0 if name == "fp64" else 10**6))
+            ms.append(p["particles"].mean(0))
+            ss.append(p["particles"].std(0))
+        post[name] = (np.array(ms), np.array(ss))
+        g.close()
+    (mm, sm), (mf, sf) = post["mixed"], post["fp64"]
+    peak = float(np.abs(mf.mean(0)).max())
+    dmean = np.abs(mm.mean(0) - mf.mean(0))
+    dstd = np.abs(sm.mean(0) - sf.mean(0))
+    se_m = np.sqrt((mm.var(0, ddof=1) + mf.var(0, ddof=1)) / 16)
+    slip = {"streams": 16, "components": int(mm.shape[1]),
+            "max_abs_mean_diff_rel_peak": float(dmean.max() / peak),
+            "max_abs_std_diff_rel_peak": float(dstd.max() / peak),
+            "max_mean_diff_over_se": float((dmean / np.maximum(se_m, 1e-12)).max()),
+            "fp64_peak_mean_slip_m": peak}
+    return {"evidence": ev, "slip_posterior_at_truth": slip}
+
+
+def nested_c2_bench(pkg, torch, cpu=True, fp64_sample=152):
+    """c2 (16x8 patches x 2 components, D = 256; 400 GNSS stations and 2000
+    InSAR points in two paths with a 5 km exponential covariance, 3200
+    observations; 2048 inner particles, ntau 50): one outer stage of the
+    4096-particle outer SMC in MIXED (timed apart from the initial
+    evaluation), FP64 against MIXED on a sample of prior geometries, and the
+    oracle's per-stage cost on the host cores."""
+    import dataclasses
+    w, obs, rg, th_true, s_true = nested_workload(pkg, "c2")
+    r = timed_outer_run(pkg, w, obs, rg, pkg.PREC_MIXED, 19, 1)
+    ss = r["stage_s"]
+    st = r["stats"]
+    out = {"workload": "c2: 16x8 patches (D=256), 400 GNSS + 2000 InSAR points (3200 obs, 5 km exponential "
+                       "covariance), 4096 outer x 2048 inner particles, ntau 50",
+           "mixed": {"outer_particles_per_s": w.n_outer / float(ss[0]), "s_outer_stage": float(ss[0]),
+                     "stage_evals": int(r["stage_evals"][0]),
+                     "nested_evals_per_s": float(r["stage_evals"][0] / ss[0]), "init_eval_s": r["init_s"],
+                     "mean_inner_stages": st["inner_stages"] / max(st["nested_evals"], 1)}}
+    # FP64 against MIXED on one wave of prior geometries
+    from smc_inversion_fort_gb300.configs import random_thetas
+    th = random_thetas(w, fp64_sample, seed=12)
+    rates = {}
+    for name, prec in (("mixed", pkg.PREC_MIXED), ("fp64", pkg.PREC_FP64)):
+        g = pkg.SmcGpu(w.settings, prec)
+        g.set_data(obs)
+        g.fault_calc_likelihood(th[:2], 5, np.arange(2, dtype=np.uint64))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nl, stt = g.fault_calc_likelihood(th, 6, np.arange(len(th), dtype=np.uint64) + 100)
+        torch.cuda.synchronize()
+        rates[name] = {"nested_evals_per_s": len(th) / (time.perf_counter() - t0), "status_max": int(stt.max()),
+                       "neglog_median": float(np.median(nl))}
+        g.close()
+    out["sample"] = {"geometries": len(th), "note": "one wave of prior geometries (one per SM), both precisions",
+                     **{k: v for k, v in rates.items()},
+                     "mixed_speedup_vs_fp64": rates["mixed"]["nested_evals_per_s"] / rates["fp64"]["nested_evals_per_s"]}
+    if cpu:
+        out["cpu_baseline"] = cpu_stage_rate(w, obs, th, out["mixed"]["mean_inner_stages"])
+        out["mixed_speedup_vs_cpu"] = out["mixed"]["outer_particles_per_s"] / out["cpu_baseline"]["value"]
+    return out
+
+
+def cpu_stage_rate(w, obs, th, mean_stages, stages=2):
+    """The oracle (timing build) on all host threads, one geometry per
+    thread, stopped after `stages` inner stages; a nested evaluation's cost
+    is that per-stage cost times the mean inner stage count of the GPU run
+    (outer particles/s = evaluations/s / 2)."""
+    import dataclasses
+    from oracle import pyoracle
+    pyoracle.build()
+    s = dataclasses.replace(w.settings, max_stages=stages)
+    o = pyoracle.Oracle(s, obs)
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    o.fault_likelihood_batch(th[:nthreads], 6, np.arange(nthreads, dtype=np.uint64) + 100, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    per_eval = dt / stages * mean_stages
+    return {"value": nthreads / per_eval / 2.0, "unit": "outer particles/s", "cores": nthreads, "kind": "port",
+            "sample": f"{nthreads} prior geometries, one per thread, first {stages} inner stages in {dt:.1f} s, "
+                      f"scaled to the GPU run's mean of {mean_stages:.1f} inner stages per evaluation"}
+
+
+def nested_c4_bench(pkg, torch, sample=152):
+    """c4 slip size (32x16 patches x 2 components, D = 1024; 400 GNSS and
+    10000 InSAR points in four paths, 11200 observations; 4096 inner
+    particles, ntau 50), MIXED on the global-matrix engine: nested
+    evaluations/s on one wave of prior geometries (one per SM)."""
+    from smc_inversion_fort_gb300.configs import random_thetas
+    w, obs, rg, th_true, s_true = nested_workload(pkg, "c4")
     g = pkg.SmcGpu(w.settings, pkg.PREC_MIXED)
     g.set_data(obs)
-    G = g.calc_greens_func(true_theta(w)[None])[0]
-    obs["dvec"] = G.T @ true_slip(w) + rng.standard_normal(G.shape[1]) * obs["obs_sigma"]
-    g.set_data(obs)
-    nsm = torch.cuda.get_device_properties(0).multi_processor_count
-    g.fault_calc_likelihood(random_thetas(w, 8, seed=11), 5, np.arange(8, dtype=np.uint64))
-    n = 4 * nsm
-    th = random_thetas(w, n, seed=12)
+    th = random_thetas(w, sample, seed=13)
+    g.stats_reset(True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    nl, st = g.fault_calc_likelihood(th, 6, np.arange(n, dtype=np.uint64) + 100)
+    nl, stt = g.fault_calc_likelihood(th, 7, np.arange(len(th), dtype=np.uint64))
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
+    st = g.stats()
     g.close()
-    out = {} if cpu else {"cpu_baseline": None,
-                          "cpu_baseline_note": "off by default (about 2.5 minutes); bench.py --c2-cpu-baseline"}
-    if cpu:
-        # the oracle on all host threads, one geometry per thread, on the first
-        # geometries of the same sample (the oracle's covariance set-up, like
-        # set_data on the GPU, is outside the timed region)
-        from oracle import pyoracle
-        pyoracle.build()
-        o = pyoracle.Oracle(w.settings, obs)
-        nthreads = os.cpu_count() or 1
-        t0 = time.perf_counter()
-        o.fault_likelihood_batch(th[:nthreads], 6, np.arange(nthreads, dtype=np.uint64) + 100, nthreads=nthreads)
-        tc = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": nthreads / tc / 2.0, "unit": "outer particles/s", "cores": nthreads,
-                               "kind": "port", "sample": f"the first {nthreads} geometries of the GPU sample, one "
-                                                         f"per thread, {tc:.1f} s wall"}
-        out["mixed_speedup_vs_cpu"] = (n / dt / 2.0) / out["cpu_baseline"]["value"]
-    return {"workload": "c2: 16x8 patches (D=256), 400 GNSS + 2000 InSAR points (3200 obs, 5 km exponential "
-                        "covariance), 2048 inner particles, ntau 50, MIXED",
-            "sample": f"{n} prior geometries in one batch (four waves of one geometry per SM)",
-            "nested_evals_per_s": n / dt, "outer_particles_per_s": n / dt / 2, "s_per_batch": dt,
-            "status_max": int(st.max()), "neglog_median": float(np.median(nl)), **out}
+    D = w.settings.dims()["D"]
+    # the global-matrix engine streams M (D^2 FP32) once per leapfrog step and
+    # A once per trajectory end: 4 D^2 (ntau + 2) bytes per trajectory
+    traj = st["inner_trajectories"]
+    gbs = traj * (w.settings.ntau + 2) * 4.0 * D * D / (st["inner_kernel_ms"] * 1e-3) / 1e9
+    return {"workload": "c4: 32x16 patches (D=1024), 400 GNSS + 10000 InSAR points (11200 obs, 5 km exponential "
+                        "covariance, 4 paths), 4096 inner particles, ntau 50, MIXED",
+            "sample": f"{len(th)} prior geometries in one batch (one per SM)", "s_per_batch": dt,
+            "nested_evals_per_s": len(th) / dt, "outer_particles_per_s": len(th) / dt / 2,
+            "status_max": int(stt.max()), "neglog_median": float(np.median(nl)),
+            "mean_inner_stages": st["inner_stages"] / max(st["nested_evals"], 1),
+            "roofline_inner": {"bound": "hbm", "achieved": gbs, "unit": "GB/s",
+                               "note": "stage matrix (FP32, D^2) streamed per leapfrog step, A per trajectory end",
+                               "inner_kernel_s": st["inner_kernel_ms"] * 1e-3}}
 
 
 def cpu_nested_rate(w, obs, rg, target_s=15.0):
-    """Oracle nested evaluations of prior-box geometries on all host threads
-    (one geometry per thread, as the reference's MPI ranks); outer particles
-    per second = evaluations per second / 2."""
+    """Oracle (timing build) nested evaluations of prior-box geometries on all
+    host threads (one geometry per thread, as the reference's MPI ranks);
+    outer particles per second = evaluations per second / 2."""
     from oracle import pyoracle
     pyoracle.build()
     o = pyoracle.Oracle(w.settings, obs)
@@ -315,7 +456,12 @@ def gb300_arm(args):
     dev = torch.device("cuda", local)
     import smc_inversion_fort_gb300 as pkg
     from smc_inversion_fort_gb300 import build as b
+    from oracle import pyoracle
+    pyoracle.use_timing_build()   # the CPU baseline legs time the -O3 build of the oracle
     b.build()
+    if args.equal_error_study:
+        equal_error_study(pkg, torch, args)
+        return
     w, obs, th = workload(args.n_theta)
     g = pkg.SmcGpu(w.settings, device=local)
     g.set_data(obs)
@@ -412,10 +558,7 @@ def gb300_arm(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded stations, prior-box geometries)",
-            "config": {"workload": "c1: 8192 geometries x 16x8 patches x 5x5 Gauss points x 400 stations (3-comp), "
-                                   "patch-constant basis, FP64",
-                       "n_theta": n, "nobs": nobs, "D": D, "entries_per_step": entries,
-                       "l2": "output 20.1 GB per step, larger than L2; no flush needed"},
+            "config": c1_config(n, nobs, D),
             "gpu_launches": 2 * args.steps,
             "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm_peak, "unit": "GB/s",
                          "frac": ach_gbs / hbm_peak, "traffic": None,
@@ -434,18 +577,62 @@ def gb300_arm(args):
         line["roofline"]["traffic_source"] = tr.get("source")
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_greens_rate(w, obs, th)
+        line["cpu_baseline"].pop("wall_s", None)
     if not args.no_nested:
         g.close()
         del out, dth
         torch.cuda.empty_cache()
-        line["nested_smc"] = nested_bench(pkg, torch, stages=args.outer_stages,
-                                          cpu=(rank == 0 and not args.no_cpu_baseline))
+        cpu = rank == 0 and not args.no_cpu_baseline
+        line["nested_smc"] = nested_bench(pkg, torch, peaks, fp64_peak, cpu=cpu, fp64_stages=args.fp64_stages)
         if not args.no_c2:
-            line["nested_smc_c2"] = nested_c2_bench(pkg, torch, cpu=(rank == 0 and args.c2_cpu_baseline))
+            line["nested_smc_c2"] = nested_c2_bench(pkg, torch, cpu=cpu)
+        if not args.no_c4:
+            line["nested_smc_c4"] = nested_c4_bench(pkg, torch)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         tdist.destroy_process_group()
+
+
+def equal_error_study(pkg, torch, args):
+    """Full c0 outer-SMC runs (fault_smc_exec to gamma = 1) over several
+    seeds in MIXED and FP64: posterior mean and std of every geometry
+    parameter, evidence, stage counts and per-stage timing, written as JSON."""
+    km, kf = (int(x) for x in args.study_seeds.split(","))
+    w, obs, rg, th_true, s_true = nested_workload(pkg, "c0")
+    runs = {"mixed": [], "fp64": []}
+    for name, prec, k in (("mixed", pkg.PREC_MIXED, km), ("fp64", pkg.PREC_FP64, kf)):
+        for seed in range(1, k + 1):
+            t0 = time.perf_counter()
+            r = timed_outer_run(pkg, w, obs, rg, prec, 1000 + seed)
+            p = r["parts"]
+            runs[name].append({"seed": 1000 + seed, "evidence": r["evidence"], "nstage": r["nstage"],
+                               "wall_s": time.perf_counter() - t0, "mean": p.mean(0).tolist(),
+                               "std": p.std(0).tolist(), "stage_s": [round(float(x), 4) for x in r["stage_s"]],
+                               "stats": r["stats"]})
+            print(name, seed, r["nstage"], r["evidence"], round(time.perf_counter() - t0, 1), flush=True)
+    summ = {}
+    for name in runs:
+        m = np.array([x["mean"] for x in runs[name]])
+        sd = np.array([x["std"] for x in runs[name]])
+        ev = np.array([x["evidence"] for x in runs[name]])
+        summ[name] = {"seeds": len(m), "mean_of_means": m.mean(0).tolist(),
+                      "se_of_means": (m.std(0, ddof=1) / np.sqrt(len(m))).tolist() if len(m) > 1 else None,
+                      "mean_of_stds": sd.mean(0).tolist(), "evidence_mean": float(ev.mean()),
+                      "evidence_se": float(ev.std(ddof=1) / np.sqrt(len(ev))) if len(ev) > 1 else None}
+    mm, mf = np.array(summ["mixed"]["mean_of_means"]), np.array(summ["fp64"]["mean_of_means"])
+    sdm, sdf = np.array(summ["mixed"]["mean_of_stds"]), np.array(summ["fp64"]["mean_of_stds"])
+    width = rg[:, 1] - rg[:, 0]
+    res = {"workload": "c0 (8x4 patches, D = 64, 60 GNSS stations, 500 outer x 500 inner particles, ntau 50)",
+           "parameters": ["x", "y", "top", "length", "width", "strike", "dip", "log_alpha2"],
+           "true_theta": th_true.tolist(), "prior_range": rg.tolist(), "runs": runs, "summary": summ,
+           "posterior_mean_rel_diff": ((mm - mf) / np.abs(mf)).tolist(),
+           "posterior_mean_diff_rel_prior_width": ((mm - mf) / width).tolist(),
+           "posterior_std_rel_diff": ((sdm - sdf) / sdf).tolist(),
+           "evidence_diff": summ["mixed"]["evidence_mean"] - summ["fp64"]["evidence_mean"]}
+    with open(args.equal_error_study, "w") as f:
+        json.dump(res, f, indent=1)
+    print(json.dumps({k: res[k] for k in ("posterior_mean_rel_diff", "posterior_std_rel_diff", "evidence_diff")}))
 
 
 def main():

@@ -14,15 +14,28 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+# timing build (-O3, FMA contraction allowed): the CPU baseline only, never a
+# parity check; select it with use_timing_build() before the first call
+FAST_LIB_PATH = os.path.join(HERE, "_build", "liboracle_fast.so")
 MAXP = 8
+_use_fast = False
 
 
 def build(force: bool = False) -> str:
     src = os.path.join(HERE, "oracle.cpp")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "oracle.h"))):
+    newest = max(os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "oracle.h")))
+    if force or any(not os.path.exists(p) or os.path.getmtime(p) < newest for p in (LIB_PATH, FAST_LIB_PATH)):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
+
+
+def use_timing_build() -> None:
+    """Load the -O3 timing build instead of the parity build (bench.py's CPU
+    baseline); must be called before any oracle call in the process."""
+    global _use_fast
+    if _lib is not None and not _use_fast:
+        raise RuntimeError("the parity build is already loaded in this process")
+    _use_fast = True
 
 
 class OrcSetup(C.Structure):
@@ -55,7 +68,8 @@ _lib = None
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
-        L = C.CDLL(build())
+        build()
+        L = C.CDLL(FAST_LIB_PATH if _use_fast else LIB_PATH)
         vp, d, i32, u64, u32 = C.c_void_p, C.c_double, C.c_int32, C.c_uint64, C.c_uint32
         L.orc_philox4x64.argtypes = [vp, vp, vp]
         L.orc_uniform.argtypes = [u64, u64, u32, u32, u64, u64]

@@ -103,7 +103,7 @@ def preset(name: str) -> Workload:
         return Workload("c2", s, 4096, 400, 2000, 2, 100.0, 1.0, 1.0, 1.0)
     if name == "c4":
         s = SmcSettings(layout=2, basis=1, nxi=(32,), neta=(16,), nquad=2, nparticle_slip=4096, sar_corr_len=5.0)
-        return Workload("c4", s, 16384, 400, 10000, 4, 100.0, 1.0, 1.0, 1.0)
+        return Workload("c4", s, 16384, 400, 10000, 8, 100.0, 1.0, 1.0, 1.0)
     if name in ("d160", "d256"):   # parity cases above 128 slip dimensions (10x8 and 16x8 patches)
         nxi = 10 if name == "d160" else 16
         s = SmcSettings(layout=2, basis=1, nxi=(nxi,), neta=(8,), nquad=2, nparticle_slip=64, ntau=20)

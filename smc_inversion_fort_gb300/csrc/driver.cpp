@@ -97,6 +97,8 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
     const smc::MeshPattern &pm = ctx->mesh;
     const int D = pm.D, N = ctx->cfg.nparticle_slip, NP2 = next_pow2(N), nd = pm.ndim_fault;
     cudaStream_t s = ctx->stream;
+    if (const char *why = smc::inner_size_limit(ctx->cfg.precision == SMCGPU_PREC_MIXED, ctx->cfg.inner_engine, D, N))
+        return ctx->fail(SMCGPU_ERR_ARG, why);
     size_t per = bytes_per_theta(ctx);
     size_t budget = (size_t)48 << 30;
     size_t freeb = 0, totb = 0;

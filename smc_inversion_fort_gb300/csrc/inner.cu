@@ -16,6 +16,14 @@ bool inner_uses_global(int mixed, int engine, int D) {
     return D > 192;
 }
 
+const char *inner_size_limit(int mixed, int engine, int D, int N) {
+    if (N > 32767) return "nparticle_slip must be < 32768";
+    if (!mixed && D > 512) return "slip dimension too large for the FP64 inner kernel (D <= 512)";
+    if (mixed && D > 1024) return "slip dimension too large for the MIXED inner kernel (D <= 1024)";
+    (void)engine;
+    return nullptr;
+}
+
 cudaError_t launch_inner(const MeshDev &m, const InnerArgs &a, cudaStream_t s, const char **why) {
     if (a.n_theta <= 0) return cudaSuccess;
     if (a.N > 32767) { *why = "nparticle_slip must be < 32768"; return cudaErrorInvalidValue; }

@@ -48,6 +48,8 @@ cudaError_t launch_gibbs(const MeshDev &m, const InnerArgs &a, cudaStream_t s);
 // true when a batch of this precision / engine / slip dimension runs on the
 // global-matrix engine (InnerArgs::mgl and ::glxc must then be set)
 bool inner_uses_global(int mixed, int engine, int D);
+// message when no inner engine takes this slip dimension / particle count (else nullptr)
+const char *inner_size_limit(int mixed, int engine, int D, int N);
 cudaError_t launch_inner(const MeshDev &m, const InnerArgs &a, cudaStream_t s, const char **why);
 
 // engine families behind launch_inner, one translation unit each
