@@ -43,6 +43,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-nested", action="store_true")
     p.add_argument("--no-c2", action="store_true", help="skip the c2 (D = 256) nested measurements")
+    p.add_argument("--no-c3", action="store_true", help="skip the c3 (per-geometry meshes) nested sample")
     p.add_argument("--no-c4", action="store_true", help="skip the c4 (D = 1024) nested sample")
     p.add_argument("--fp64-stages", type=int, default=3, help="c0 outer stages timed in FP64")
     p.add_argument("--equal-error-study", type=str, default=None, metavar="OUT_JSON",
@@ -194,17 +195,18 @@ def load_traffic():
 def nested_workload(pkg, name="c0", seed=2024):
     """Seeded observations of a named workload, data from its known fault
     (the GPU Green's build of the true geometry plus Gaussian noise)."""
-    from smc_inversion_fort_gb300.configs import make_stations, preset, prior_range, true_slip, true_theta
+    from smc_inversion_fort_gb300.configs import fixed_mesh, make_stations, preset, prior_range, true_slip, true_theta
     w = preset(name)
     rng = np.random.default_rng(seed)
     obs = make_stations(w, rng)
     obs["dvec"] = np.zeros(len(obs["obs_sigma"]))
-    g = pkg.SmcGpu(w.settings)
+    wf = fixed_mesh(w, true_theta(w))   # the true geometry's own mesh (per-geometry meshes)
+    g = pkg.SmcGpu(wf.settings)
     g.set_data(obs)
     G = g.calc_greens_func(true_theta(w)[None])[0]
     g.close()
-    obs["dvec"] = G.T @ true_slip(w) + rng.standard_normal(G.shape[1]) * obs["obs_sigma"]
-    return w, obs, prior_range(w), true_theta(w), true_slip(w)
+    obs["dvec"] = G.T @ true_slip(wf) + rng.standard_normal(G.shape[1]) * obs["obs_sigma"]
+    return w, obs, prior_range(w), true_theta(w), true_slip(wf)
 
 
 def inner_roofline(st, ntau, D, peak, peak_name):
@@ -424,6 +426,42 @@ def nested_c4_bench(pkg, torch, sample=152):
                                "inner_kernel_s": st["inner_kernel_ms"] * 1e-3}}
 
 
+def nested_c3_bench(pkg, torch, sample=304, fp64_sample=152):
+    """c3: per-geometry meshes (2.5 km patches on a 10-60 km x 5-30 km
+    rectangle: 4x2 ... 24x12 patches, D = 16 ... 576) with the c2
+    observations and 2048 inner particles, engines from the autotuner's
+    table (SMCGPU_ENGINE_AUTO): nested evaluations/s of one uneven batch of
+    prior geometries in MIXED and FP64 (each call splits the batch by mesh
+    and runs the parts concurrently)."""
+    from smc_inversion_fort_gb300.configs import mesh_of, random_thetas
+    w, obs, rg, th_true, s_true = nested_workload(pkg, "c3")
+    th = random_thetas(w, sample, seed=14)
+    D = np.array([2 * np.prod(mesh_of(w.settings, t)) for t in th])
+    out = {"workload": "c3: 2.5 km patches on 10-60 x 5-30 km rectangles (4x2 ... 24x12 patches, D 16-576), "
+                       "400 GNSS + 2000 InSAR points (3200 obs), 2048 inner particles, ntau 50, engines from "
+                       "the autotuner's table",
+           "sample": f"{sample} prior geometries (MIXED), the first {fp64_sample} (FP64)",
+           "meshes_in_sample": int(len({mesh_of(w.settings, t) for t in th})),
+           "D_min_median_max": [int(D.min()), float(np.median(D)), int(D.max())]}
+    for name, prec, n in (("mixed", pkg.PREC_MIXED, sample), ("fp64", pkg.PREC_FP64, fp64_sample)):
+        g = pkg.SmcGpu(w.settings, prec)
+        g.set_data(obs)
+        g.fault_calc_likelihood(th[:n], 5, np.arange(n, dtype=np.uint64))   # meshes' contexts and buffers
+        g.stats_reset(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nl, st = g.fault_calc_likelihood(th[:n], 6, np.arange(n, dtype=np.uint64) + 1000)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        stt = g.stats()
+        g.close()
+        out[name] = {"nested_evals_per_s": n / dt, "outer_particles_per_s": n / dt / 2, "s_per_batch": dt,
+                     "status_max": int(st.max()), "mean_inner_stages": stt["inner_stages"] / max(stt["nested_evals"], 1)}
+    # the same geometries in both precisions: the FP64 sample's MIXED rate
+    out["mixed_speedup_vs_fp64"] = out["mixed"]["nested_evals_per_s"] / out["fp64"]["nested_evals_per_s"]
+    return out
+
+
 def cpu_nested_rate(w, obs, rg, target_s=15.0):
     """Oracle (timing build) nested evaluations of prior-box geometries on all
     host threads (one geometry per thread, as the reference's MPI ranks);
@@ -586,6 +624,8 @@ def gb300_arm(args):
         line["nested_smc"] = nested_bench(pkg, torch, peaks, fp64_peak, cpu=cpu, fp64_stages=args.fp64_stages)
         if not args.no_c2:
             line["nested_smc_c2"] = nested_c2_bench(pkg, torch, cpu=cpu)
+        if not args.no_c3:
+            line["nested_smc_c3"] = nested_c3_bench(pkg, torch)
         if not args.no_c4:
             line["nested_smc_c4"] = nested_c4_bench(pkg, torch)
     if rank == 0:

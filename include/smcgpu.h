@@ -75,9 +75,13 @@ extern "C" {
 #define SMCGPU_ENGINE_CUDA     1   /* FP32 FMA on CUDA cores                            */
 #define SMCGPU_ENGINE_TCGEN05  2   /* BF16x3 tcgen05.mma with a tensor-memory accumulator */
 #define SMCGPU_ENGINE_GLOBAL   3   /* stage matrix in global memory, streamed once per
-                                      leapfrog step; any slip dimension up to 1024 (MIXED,
-                                      FP32 FMA) or 512 (FP64).  The other engines fall back
-                                      to it above their own limits.                     */
+                                      leapfrog step; any slip dimension up to 1024 (FP32
+                                      FMA in MIXED, FP64 FMA in FP64).  The other engines
+                                      fall back to it above their own limits.           */
+#define SMCGPU_ENGINE_AUTO     4   /* per slip dimension from the engine table
+                                      (smcgpu_set_engine_table; the package's autotuner
+                                      writes one), else MMA / CUDA cores up to their
+                                      limits and the global-matrix engine above        */
 
 typedef struct smcgpu_config {
     int32_t layout;
@@ -112,8 +116,18 @@ typedef struct smcgpu_config {
                                       128), CUDA cores (<= 192), tcgen05 (<= 128), or the
                                       global-matrix engine (<= 1024; also the fallback
                                       above each engine's limit).  FP64: CUDA cores up to
-                                      128, the global-matrix engine up to 512 (or at any
+                                      128, the global-matrix engine up to 1024 (or at any
                                       size with SMCGPU_ENGINE_GLOBAL).                  */
+    double patch_km;               /* > 0 (LAYOUT_RECT only): a patch size; each geometry
+                                      gets its own mesh, nxi = round(length / patch_km)
+                                      and neta = round(width / patch_km), clamped to
+                                      [2, nxi[0]] and [2, neta[0]], so one batch mixes
+                                      patch counts (and slip dimensions).  0: the fixed
+                                      mesh nxi[0] x neta[0] of every geometry.  With
+                                      per-geometry meshes the nested evaluation and the
+                                      outer SMC run as usual; the calls that return
+                                      per-geometry matrices (Green's, Gram, slip
+                                      populations) need a fixed mesh.                   */
 } smcgpu_config;
 
 typedef struct smcgpu_ctx smcgpu_ctx;
@@ -336,6 +350,15 @@ int32_t smcgpu_write_point_cloud(smcgpu_ctx *ctx, const char *prefix, int32_t n,
 /* Last error message of the context (or, when ctx is NULL, of the last
  * create call or file reader on this thread). */
 const char *smcgpu_last_error(const smcgpu_ctx *ctx);
+
+/* Engine table for SMCGPU_ENGINE_AUTO (no counterpart in the reference): for
+ * slip dimensions D <= dmax[k] (ascending), engine[k] (SMCGPU_ENGINE_MMA ..
+ * _GLOBAL) with warps[k] warps per geometry (CUDA-core engine; 0 = from the
+ * batch size).  precision: SMCGPU_PREC_FP64 or SMCGPU_PREC_MIXED; n = 0
+ * clears the table.  The package's autotuner times the candidates per slip
+ * dimension on the device and writes the table it loads. */
+int32_t smcgpu_set_engine_table(smcgpu_ctx *ctx, int32_t precision, int32_t n, const int32_t *dmax,
+                                const int32_t *engine, const int32_t *warps);
 
 /* ---- run statistics (no counterpart in the reference, which prints only the
  * wall time of one nested evaluation, main.f90:464-480) ----

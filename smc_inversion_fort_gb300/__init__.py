@@ -25,7 +25,9 @@ PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
 ST_BISECT_CAP, ST_STAGE_CAP, ST_NONFINITE, ST_NEWTON_CAP, ST_REFLECT_CAP, ST_TUNE_COUNT = 1, 2, 4, 8, 16, 32
 ST_WAIT_CAP = 64
 ST_SNAPSHOT_IO = 128
-ENGINE_MMA, ENGINE_CUDA, ENGINE_TCGEN05, ENGINE_GLOBAL = 0, 1, 2, 3
+ENGINE_MMA, ENGINE_CUDA, ENGINE_TCGEN05, ENGINE_GLOBAL, ENGINE_AUTO = 0, 1, 2, 3, 4
+# engine table written by the autotuner (autotune.py), loaded under ENGINE_AUTO
+ENGINE_TABLE_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "engine_table.json")
 
 
 class SmcConfig(C.Structure):
@@ -41,7 +43,7 @@ class SmcConfig(C.Structure):
         ("max_stages", C.c_int32),
         ("cv_inner", C.c_double), ("cv_outer", C.c_double), ("sar_corr_len", C.c_double),
         ("precision", C.c_int32), ("device", C.c_int32), ("max_outer_stages", C.c_int32),
-        ("inner_warps", C.c_int32), ("inner_engine", C.c_int32),
+        ("inner_warps", C.c_int32), ("inner_engine", C.c_int32), ("patch_km", C.c_double),
     ]
 
 
@@ -114,6 +116,7 @@ def load_library() -> C.CDLL:
         "smcgpu_stats_reset": (i32, [vp, i32]),
         "smcgpu_stats_get": (i32, [vp, P(Stats)]),
         "smcgpu_outer_stage_times": (i32, [vp, i32, vp, vp, P(i32)]),
+        "smcgpu_set_engine_table": (i32, [vp, i32, i32, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -134,6 +137,7 @@ EXPORTED_SYMBOLS = [
     "smcgpu_read_observations", "smcgpu_read_range", "smcgpu_read_values", "smcgpu_write_slip",
     "smcgpu_slip_map", "smcgpu_slip_to_nodes", "smcgpu_write_slip_map", "smcgpu_point_cloud",
     "smcgpu_write_point_cloud", "smcgpu_stats_reset", "smcgpu_stats_get", "smcgpu_outer_stage_times",
+    "smcgpu_set_engine_table",
 ]
 
 
@@ -178,7 +182,18 @@ def make_config(s: SmcSettings, precision: int = PREC_FP64, device: int = 0) -> 
     cfg.max_outer_stages = s.max_outer_stages
     cfg.inner_warps = s.inner_warps
     cfg.inner_engine = s.inner_engine
+    cfg.patch_km = s.patch_km
     return cfg
+
+
+def load_engine_table(path: str = ENGINE_TABLE_PATH):
+    """The autotuner's engine table: {"fp64": [[dmax, engine, warps], ...], "mixed": [...]}
+    or None when there is none."""
+    import json
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f)
 
 
 class SmcGpu:
@@ -197,6 +212,19 @@ class SmcGpu:
             raise SmcError(f"smcgpu_create failed ({rc}): {self.lib.smcgpu_last_error(None).decode()}")
         self.h = h
         self.nobs = 0
+        if settings.inner_engine == ENGINE_AUTO:
+            tab = load_engine_table()
+            if tab:
+                for key, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+                    if tab.get(key):
+                        self.set_engine_table(prec, tab[key])
+
+    def set_engine_table(self, precision: int, rows):
+        """rows: [(dmax, engine, warps), ...] with dmax ascending (SMCGPU_ENGINE_AUTO)."""
+        a = np.ascontiguousarray(np.asarray(rows, dtype=np.int32).reshape(-1, 3).T)
+        dm, en, wa = (np.ascontiguousarray(a[i]) for i in range(3))
+        self._check(self.lib.smcgpu_set_engine_table(self.h, precision, len(dm), _ptr(dm), _ptr(en), _ptr(wa)),
+                    "set_engine_table")
 
     def close(self):
         if getattr(self, "h", None):

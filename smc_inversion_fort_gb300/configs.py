@@ -39,7 +39,8 @@ class SmcSettings:
     sar_corr_len: float = 10.0
     max_outer_stages: int = 0
     inner_warps: int = 0          # GPU inner kernel: warps per geometry (0: by batch size)
-    inner_engine: int = 0         # inner step engine: 0 warp MMA, 1 CUDA cores, 2 tcgen05, 3 global matrix
+    inner_engine: int = 0         # inner step engine: 0 warp MMA, 1 CUDA cores, 2 tcgen05, 3 global matrix, 4 auto
+    patch_km: float = 0.0         # > 0: per-geometry meshes of this patch size (rectangle layout)
 
     def ndim_fault(self) -> int:
         if self.layout == 0:
@@ -68,6 +69,14 @@ class SmcSettings:
 RECT_RANGE = np.array([[-20.0, 20.0], [-20.0, 20.0], [0.0, 10.0], [10.0, 40.0], [5.0, 20.0],
                        [0.0, 360.0], [10.0, 90.0], [-10.0, 2.0]])
 RECT_TRUE = np.array([2.0, -3.0, 2.0, 24.0, 12.0, 30.0, 45.0, -3.0])
+# per-geometry meshes: length 10-60 km, width 5-30 km (c3); 4-12 km x 4-8 km (tiny-uneven)
+C3_RANGE = RECT_RANGE.copy()
+C3_RANGE[3] = [10.0, 60.0]
+C3_RANGE[4] = [5.0, 30.0]
+TINY_UNEVEN_RANGE = RECT_RANGE.copy()
+TINY_UNEVEN_RANGE[3] = [4.0, 12.0]
+TINY_UNEVEN_RANGE[4] = [4.0, 8.0]
+TINY_UNEVEN_TRUE = np.array([2.0, -3.0, 2.0, 8.0, 6.0, 30.0, 45.0, -3.0])
 
 
 @dataclasses.dataclass
@@ -101,6 +110,16 @@ def preset(name: str) -> Workload:
     if name == "c2":
         s = SmcSettings(layout=2, basis=1, nxi=(16,), neta=(8,), nquad=2, nparticle_slip=2048, sar_corr_len=5.0)
         return Workload("c2", s, 4096, 400, 2000, 2, 100.0, 1.0, 1.0, 1.0)
+    if name == "c3":
+        # uneven patch counts: 2.5 km patches on a 10-60 km x 5-30 km rectangle
+        # give 4x2 ... 24x12 patches (D = 16 ... 576) per geometry; data as c2
+        s = SmcSettings(layout=2, basis=1, nxi=(24,), neta=(12,), nquad=2, nparticle_slip=2048, sar_corr_len=5.0,
+                        patch_km=2.5, inner_engine=4)
+        return Workload("c3", s, 4096, 400, 2000, 2, 100.0, 1.0, 1.0, 1.0)
+    if name == "tiny-uneven":
+        # per-geometry meshes small enough for the oracle: 2 km patches, 2x2 ... 6x4
+        s = SmcSettings(layout=2, basis=1, nxi=(6,), neta=(4,), nquad=2, nparticle_slip=64, patch_km=2.0)
+        return Workload("tiny-uneven", s, 16, 12, 0, 0, 60.0, 0.2, 0.5, 1.0)
     if name == "c4":
         s = SmcSettings(layout=2, basis=1, nxi=(32,), neta=(16,), nquad=2, nparticle_slip=4096, sar_corr_len=5.0)
         return Workload("c4", s, 16384, 400, 10000, 8, 100.0, 1.0, 1.0, 1.0)
@@ -162,6 +181,8 @@ def _trace_truth(s: SmcSettings):
 
 def true_theta(w: Workload) -> np.ndarray:
     s = w.settings
+    if w.name == "tiny-uneven":
+        return TINY_UNEVEN_TRUE.copy()
     if s.layout == 2:
         t = RECT_TRUE.copy()
         if s.rect_hyper:
@@ -180,6 +201,10 @@ def true_theta(w: Workload) -> np.ndarray:
 
 def prior_range(w: Workload) -> np.ndarray:
     s = w.settings
+    if w.name == "c3":
+        return C3_RANGE.copy()
+    if w.name == "tiny-uneven":
+        return TINY_UNEVEN_RANGE.copy()
     if s.layout == 2:
         r = RECT_RANGE.copy()
         if s.rect_hyper:
@@ -291,3 +316,23 @@ def random_thetas(w: Workload, n: int, seed: int = 7) -> np.ndarray:
     rng = np.random.default_rng(seed)
     r = prior_range(w)
     return r[:, 0] + rng.uniform(0.0, 1.0, (n, len(r))) * (r[:, 1] - r[:, 0])
+
+
+def mesh_of(s: SmcSettings, theta) -> tuple:
+    """Patch counts of a rectangle geometry under per-geometry meshes
+    (patch_km > 0): round(length / patch_km) x round(width / patch_km),
+    clamped to [2, nxi[0]] x [2, neta[0]]; the fixed mesh otherwise."""
+    if s.patch_km <= 0:
+        return s.nxi[0], s.neta[0]
+
+    def count(v, mx):
+        if not np.isfinite(v) or v <= 0:
+            return 2
+        return int(min(max(np.floor(v / s.patch_km + 0.5), 2), mx))
+    return count(theta[3], s.nxi[0]), count(theta[4], s.neta[0])
+
+
+def fixed_mesh(w: Workload, theta) -> Workload:
+    """The workload with the fixed mesh of geometry theta (per-geometry meshes off)."""
+    nx, ne = mesh_of(w.settings, theta)
+    return dataclasses.replace(w, settings=dataclasses.replace(w.settings, nxi=(nx,), neta=(ne,), patch_km=0.0))

@@ -105,8 +105,11 @@ extern "C" int32_t smcgpu_create(const smcgpu_config *cfg, smcgpu_ctx **out) {
     if (e.empty() && cfg->inner_warps != 0 && cfg->inner_warps != 1 && cfg->inner_warps != 2 &&
         cfg->inner_warps != 4 && cfg->inner_warps != 8)
         e = "inner_warps must be 0, 1, 2, 4 or 8";
-    if (e.empty() && (cfg->inner_engine < SMCGPU_ENGINE_MMA || cfg->inner_engine > SMCGPU_ENGINE_GLOBAL))
-        e = "inner_engine must be SMCGPU_ENGINE_MMA, _CUDA, _TCGEN05 or _GLOBAL";
+    if (e.empty() && (cfg->inner_engine < SMCGPU_ENGINE_MMA || cfg->inner_engine > SMCGPU_ENGINE_AUTO))
+        e = "inner_engine must be SMCGPU_ENGINE_MMA, _CUDA, _TCGEN05, _GLOBAL or _AUTO";
+    if (e.empty() && !(cfg->patch_km >= 0.0)) e = "patch_km must be >= 0";
+    if (e.empty() && cfg->patch_km > 0.0 && cfg->layout != SMCGPU_LAYOUT_RECT)
+        e = "per-geometry meshes (patch_km > 0) need the rectangle layout";
     if (!e.empty()) { g_create_err = e; delete ctx; return SMCGPU_ERR_ARG; }
     cudaError_t ce = cudaSetDevice(cfg->device);
     if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, cfg->device);
@@ -148,8 +151,79 @@ extern "C" int32_t smcgpu_create(const smcgpu_config *cfg, smcgpu_ctx **out) {
     return SMCGPU_OK;
 }
 
+int smc_child_context(smcgpu_ctx *parent, int nxi, int neta, smcgpu_ctx **out) {
+    const long long key = (long long)nxi * 4096 + neta;
+    auto it = parent->children.find(key);
+    if (it != parent->children.end()) {
+        *out = it->second;
+        return SMCGPU_OK;
+    }
+    smcgpu_config c = parent->cfg;
+    c.nxi[0] = nxi;
+    c.neta[0] = neta;
+    c.patch_km = 0.0;
+    smcgpu_ctx *ch = nullptr;
+    int r = smcgpu_create(&c, &ch);
+    if (r != SMCGPU_OK)
+        return parent->fail(r, "mesh " + std::to_string(nxi) + "x" + std::to_string(neta) + ": " + g_create_err);
+    ch->parent = parent;
+    for (int k = 0; k < 2; ++k) {
+        ch->eng_dmax[k] = parent->eng_dmax[k];
+        ch->eng_engine[k] = parent->eng_engine[k];
+        ch->eng_warps[k] = parent->eng_warps[k];
+    }
+    ch->nobs = parent->nobs; ch->nsar = parent->nsar; ch->ngnss = parent->ngnss; ch->npath = parent->npath;
+    ch->nstation = parent->nstation;
+    ch->nsar_index0 = parent->nsar_index0;
+    ch->dsd_sar = parent->dsd_sar;
+    ch->dsd_gnss = parent->dsd_gnss;
+    ch->has_data = true;
+    refresh_md(ch);
+    const smc::MeshDev &pm = parent->md;
+    smc::MeshDev &m = ch->md;
+    m.st_x = pm.st_x; m.st_y = pm.st_y; m.st_row = pm.st_row; m.st_nrow = pm.st_nrow;
+    m.obs_e = pm.obs_e; m.obs_sigma = pm.obs_sigma; m.dvec = pm.dvec;
+    m.nsar_index = pm.nsar_index; m.sar_inv = pm.sar_inv; m.sar_off = pm.sar_off;
+    parent->children[key] = ch;
+    *out = ch;
+    return SMCGPU_OK;
+}
+
+void smc_drop_children(smcgpu_ctx *ctx) {
+    for (auto &kv : ctx->children) smcgpu_destroy(kv.second);
+    ctx->children.clear();
+}
+
+extern "C" int32_t smcgpu_set_engine_table(smcgpu_ctx *ctx, int32_t precision, int32_t n, const int32_t *dmax,
+                                           const int32_t *engine, const int32_t *warps) {
+    if (!ctx) return SMCGPU_ERR_ARG;
+    if (precision != SMCGPU_PREC_FP64 && precision != SMCGPU_PREC_MIXED)
+        return ctx->fail(SMCGPU_ERR_ARG, "engine table: precision must be FP64 or MIXED");
+    if (n < 0 || (n > 0 && (!dmax || !engine || !warps))) return ctx->fail(SMCGPU_ERR_ARG, "engine table: bad arguments");
+    const int pi = precision == SMCGPU_PREC_MIXED ? 1 : 0;
+    for (int k = 0; k < n; ++k) {
+        if (k > 0 && dmax[k] <= dmax[k - 1]) return ctx->fail(SMCGPU_ERR_ARG, "engine table: dmax must ascend");
+        if (engine[k] < SMCGPU_ENGINE_MMA || engine[k] > SMCGPU_ENGINE_GLOBAL)
+            return ctx->fail(SMCGPU_ERR_ARG, "engine table: engine must be MMA, CUDA, TCGEN05 or GLOBAL");
+        if (pi == 0 && engine[k] != SMCGPU_ENGINE_CUDA && engine[k] != SMCGPU_ENGINE_GLOBAL)
+            return ctx->fail(SMCGPU_ERR_ARG, "engine table: FP64 runs on the CUDA-core or global-matrix engine");
+        if (warps[k] != 0 && warps[k] != 1 && warps[k] != 2 && warps[k] != 4 && warps[k] != 8)
+            return ctx->fail(SMCGPU_ERR_ARG, "engine table: warps must be 0, 1, 2, 4 or 8");
+    }
+    ctx->eng_dmax[pi].assign(dmax, dmax + n);
+    ctx->eng_engine[pi].assign(engine, engine + n);
+    ctx->eng_warps[pi].assign(warps, warps + n);
+    for (auto &kv : ctx->children) {
+        kv.second->eng_dmax[pi] = ctx->eng_dmax[pi];
+        kv.second->eng_engine[pi] = ctx->eng_engine[pi];
+        kv.second->eng_warps[pi] = ctx->eng_warps[pi];
+    }
+    return SMCGPU_OK;
+}
+
 extern "C" int32_t smcgpu_destroy(smcgpu_ctx *ctx) {
     if (!ctx) return SMCGPU_OK;
+    smc_drop_children(ctx);
     cudaSetDevice(ctx->cfg.device);
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
@@ -208,6 +282,7 @@ extern "C" int32_t smcgpu_set_data(smcgpu_ctx *ctx, int32_t nobs, const double *
     if (!ctx) return SMCGPU_ERR_ARG;
     if (nobs <= 0 || !obs_points || !obs_unitvec || !obs_sigma || !dvec || npath < 0 || ngnss < 0)
         return ctx->fail(SMCGPU_ERR_ARG, "set_data: invalid arguments");
+    smc_drop_children(ctx);   // they borrow the observation buffers about to be replaced
     if (npath > 0 && !nsar_index) return ctx->fail(SMCGPU_ERR_ARG, "set_data: nsar_index missing");
     CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
     std::vector<int> idx0(npath + 1, 0);

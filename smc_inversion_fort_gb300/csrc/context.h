@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -19,6 +20,13 @@ std::string fortran_f(double v, int w, int d);
 // "mkdir -p" of a path (the reference shells out to it, main.f90:202-207)
 void mkdir_p(const std::string &path);
 }
+struct smcgpu_ctx;
+// per-geometry meshes: the child context of mesh nxi x neta (made on first
+// use; it shares the parent's observations) and the release of all children
+int smc_child_context(smcgpu_ctx *parent, int nxi, int neta, smcgpu_ctx **out);
+void smc_drop_children(smcgpu_ctx *ctx);
+// step engine and warps per geometry of a context's batches (SMCGPU_ENGINE_AUTO resolved)
+void smc_resolve_engine(const smcgpu_ctx *ctx, int *engine, int *warps);
 
 struct smcgpu_ctx {
     smcgpu_config cfg;
@@ -73,9 +81,20 @@ struct smcgpu_ctx {
         long long evals = 0;
         smc::DevBuf<unsigned long long> d_counters;    // [0] stages, [1] trajectories
     } stats;
+    // per-geometry meshes (cfg.patch_km > 0): one child context per mesh, made
+    // on first use; a child borrows the parent's observation buffers
+    smcgpu_ctx *parent = nullptr;
+    std::map<long long, smcgpu_ctx *> children;
+    // engine table of SMCGPU_ENGINE_AUTO, per precision (0 FP64, 1 MIXED)
+    std::vector<int> eng_dmax[2], eng_engine[2], eng_warps[2];
     // per-stage wall seconds and nested evaluations of the last fault_smc_exec
     std::vector<double> outer_stage_s;
     std::vector<long long> outer_stage_evals;
+
+    // the whitened-observation tables of the gram kernel (a child context
+    // borrows its parent's)
+    const double *obs_roww() const { return parent ? parent->d_roww.p : d_roww.p; }
+    const double *obs_dx() const { return parent ? parent->d_dx.p : d_dx.p; }
 
     int fail(int code, const std::string &msg) {
         err = msg;

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -36,10 +37,37 @@ int next_pow2(int n) {
     return p;
 }
 
+}  // namespace
+
+// The step engine and warps per geometry of this context's batches: the
+// configured engine, or under SMCGPU_ENGINE_AUTO the engine table's entry for
+// the slip dimension (default: warp MMA / CUDA cores up to their limits, the
+// global-matrix engine above).
+void smc_resolve_engine(const smcgpu_ctx *ctx, int *engine, int *warps) {
+    *engine = ctx->cfg.inner_engine;
+    *warps = ctx->cfg.inner_warps;
+    if (*engine != SMCGPU_ENGINE_AUTO) return;
+    const int D = ctx->mesh.D, pi = ctx->cfg.precision == SMCGPU_PREC_MIXED ? 1 : 0;
+    const std::vector<int> &dm = ctx->eng_dmax[pi];
+    for (size_t k = 0; k < dm.size(); ++k)
+        if (D <= dm[k]) {
+            *engine = ctx->eng_engine[pi][k];
+            *warps = ctx->eng_warps[pi][k];
+            return;
+        }
+    *engine = pi ? (D <= 256 ? SMCGPU_ENGINE_MMA : SMCGPU_ENGINE_GLOBAL)
+                 : (D <= 128 ? SMCGPU_ENGINE_CUDA : SMCGPU_ENGINE_GLOBAL);
+    *warps = 0;
+}
+
+namespace {
+
 // streamed stage matrix of the warp-MMA inner engine: uint4 per geometry (0 when unused)
 size_t afrag_per_theta(const smcgpu_ctx *ctx) {
     const int D = ctx->mesh.D;
-    const bool streamed = ctx->cfg.precision == SMCGPU_PREC_MIXED && ctx->cfg.inner_engine == SMCGPU_ENGINE_MMA &&
+    int engine, warps;
+    smc_resolve_engine(ctx, &engine, &warps);
+    const bool streamed = ctx->cfg.precision == SMCGPU_PREC_MIXED && engine == SMCGPU_ENGINE_MMA &&
                           D > 128 && D <= 256;
     return streamed ? (size_t)256 * 256 / 4 : 0;
 }
@@ -50,7 +78,9 @@ size_t gl_bytes_per_theta(const smcgpu_ctx *ctx, size_t *mgl, size_t *glxc) {
     const int D = ctx->mesh.D;
     const bool mixed = ctx->cfg.precision == SMCGPU_PREC_MIXED;
     const size_t el = mixed ? sizeof(float) : sizeof(double);
-    const bool on = smc::inner_uses_global(mixed, ctx->cfg.inner_engine, D);
+    int engine, warps;
+    smc_resolve_engine(ctx, &engine, &warps);
+    const bool on = smc::inner_uses_global(mixed, engine, D);
     *mgl = on ? (size_t)D * D * el : 0;
     *glxc = on ? (size_t)16 * D * el : 0;
     return *mgl + *glxc;
@@ -144,7 +174,7 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
         CU(smc::launch_greens(ctx->md, nb, ctx->d_planes.p, SMCGPU_PREC_FP64, ctx->d_gmat.p, s), "greens kernel");
         CU(smc::launch_setup(ctx->md, nb, th, ctx->d_planes.p, ctx->d_lval.p, ctx->d_ltval.p, ctx->d_llval.p,
                              ctx->d_aux.p, s), "setup kernel");
-        CU(smc::launch_gram(ctx->md, nb, ctx->d_gmat.p, ctx->d_roww.p, ctx->d_dx.p, ctx->d_aux.p, ctx->dsd_sar,
+        CU(smc::launch_gram(ctx->md, nb, ctx->d_gmat.p, ctx->obs_roww(), ctx->obs_dx(), ctx->d_aux.p, ctx->dsd_sar,
                             ctx->dsd_gnss, ctx->d_A.p, ctx->d_b.p, ctx->d_dsd.p, ctx->d_gw.p, s), "gram kernel");
         CU(cudaMemsetAsync(status_dev + t0, 0, (size_t)nb * sizeof(int), s), "memset");
         CU(cudaMemsetAsync(ctx->d_ibuf.p, 0, (size_t)nb * 4 * NP2 * sizeof(int), s), "memset");
@@ -171,9 +201,9 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
         a.glxc = glxc_b ? (void *)ctx->d_glxc.p : nullptr;
         CU(ctx->d_queue.ensure(1), "alloc queue");
         a.queue = ctx->d_queue.p;
-        a.warps_per_theta = ctx->cfg.inner_warps;
-        a.engine = ctx->cfg.inner_engine;
+        smc_resolve_engine(ctx, &a.engine, &a.warps_per_theta);
         a.counters = stats.on ? stats.d_counters.p : nullptr;
+        if (ctx->parent && ctx->parent->stats.on) a.counters = ctx->parent->stats.d_counters.p;
         if (stats.on) CU(stats_mark(stats.inner_ev, s), "stats event");
         cudaError_t e = smc::launch_inner(ctx->md, a, s, &why);
         if (e != cudaSuccess) {
@@ -222,7 +252,7 @@ int gram_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, double *gsg, dou
         CU(smc::launch_greens(ctx->md, nb, ctx->d_planes.p, SMCGPU_PREC_FP64, ctx->d_gmat.p, s), "greens kernel");
         CU(smc::launch_setup(ctx->md, nb, th, ctx->d_planes.p, ctx->d_lval.p, ctx->d_ltval.p, ctx->d_llval.p,
                              ctx->d_aux.p, s), "setup kernel");
-        CU(smc::launch_gram(ctx->md, nb, ctx->d_gmat.p, ctx->d_roww.p, ctx->d_dx.p, ctx->d_aux.p, ctx->dsd_sar,
+        CU(smc::launch_gram(ctx->md, nb, ctx->d_gmat.p, ctx->obs_roww(), ctx->obs_dx(), ctx->d_aux.p, ctx->dsd_sar,
                             ctx->dsd_gnss, ctx->d_A.p, ctx->d_b.p, ctx->d_dsd.p, ctx->d_gw.p, s), "gram kernel");
         CU(cudaMemcpyAsync(gsg + (size_t)t0 * D * D, ctx->d_A.p, (size_t)nb * D * D * sizeof(double),
                            cudaMemcpyDeviceToHost, s), "copy gsgmat");
@@ -231,6 +261,114 @@ int gram_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, double *gsg, dou
         CU(cudaMemcpyAsync(dsd + t0, ctx->d_dsd.p, (size_t)nb * sizeof(double), cudaMemcpyDeviceToHost, s), "copy dsd");
         CU(cudaStreamSynchronize(s), "sync");
     }
+    return SMCGPU_OK;
+}
+
+// Per-geometry meshes (cfg.patch_km > 0): the patch counts of a rectangle
+// geometry, nxi = round(length / patch_km), neta = round(width / patch_km),
+// clamped to [2, nxi[0]] and [2, neta[0]] (a non-finite size gives 2).
+void mesh_of(const smcgpu_ctx *ctx, const double *th, int *nx, int *ne) {
+    const double ps = ctx->cfg.patch_km;
+    auto count = [&](double len, int mx) {
+        if (!(len > 0.0) || !std::isfinite(len)) return 2;
+        const double v = std::floor(len / ps + 0.5);
+        return (int)std::min<double>(std::max<double>(v, 2.0), (double)mx);
+    };
+    *nx = count(th[3], ctx->cfg.nxi[0]);
+    *ne = count(th[4], ctx->cfg.neta[0]);
+}
+
+// Nested evaluations of host geometries under per-geometry meshes: the batch
+// is split by mesh, each part runs the usual device pipeline in its mesh's
+// child context on that context's own stream (all parts launched before any
+// is waited for, costliest first), and the results return in the caller's
+// order.
+int uneven_eval(smcgpu_ctx *ctx, int n, const double *theta, uint64_t seed, const unsigned long long *streams,
+                double *neglog, int32_t *status, int32_t *nstage, double *tg, double *ti) {
+    const int nd = ctx->mesh.ndim_fault, ms = ctx->cfg.max_stages + 2;
+    struct Part {
+        int nx = 0, ne = 0;
+        std::vector<int> idx;
+        std::vector<double> th;
+        std::vector<unsigned long long> sid;
+        smcgpu_ctx *ch = nullptr;
+    };
+    std::map<long long, Part> parts;
+    for (int i = 0; i < n; ++i) {
+        int nx, ne;
+        mesh_of(ctx, theta + (size_t)i * nd, &nx, &ne);
+        Part &p = parts[(long long)nx * 4096 + ne];
+        p.nx = nx;
+        p.ne = ne;
+        p.idx.push_back(i);
+    }
+    std::vector<Part *> order;
+    for (auto &kv : parts) order.push_back(&kv.second);
+    // costliest first: the inner step cost grows as D^2, D = 2 nx ne
+    std::stable_sort(order.begin(), order.end(), [](const Part *a, const Part *b) {
+        const double ca = (double)a->nx * a->ne * a->nx * a->ne * a->idx.size();
+        const double cb = (double)b->nx * b->ne * b->nx * b->ne * b->idx.size();
+        return ca > cb;
+    });
+    const bool want_ns = nstage || tg || ti, want_tr = tg || ti;
+    for (Part *p : order) {
+        int r = smc_child_context(ctx, p->nx, p->ne, &p->ch);
+        if (r) return r;
+        smcgpu_ctx *ch = p->ch;
+        const int ng = (int)p->idx.size();
+        p->th.resize((size_t)ng * nd);
+        p->sid.resize(ng);
+        for (int q = 0; q < ng; ++q) {
+            std::memcpy(&p->th[(size_t)q * nd], theta + (size_t)p->idx[q] * nd, nd * sizeof(double));
+            p->sid[q] = streams[p->idx[q]];
+        }
+        cudaStream_t cs = ch->stream;
+        CU(ch->d_theta.upload(p->th.data(), p->th.size(), cs), "upload theta");
+        CU(ch->d_streams.upload(p->sid.data(), ng, cs), "upload streams");
+        CU(ch->d_neglog.ensure(ng), "alloc");
+        CU(ch->d_status.ensure(ng), "alloc");
+        NestedOpts opt;
+        if (want_ns) {
+            CU(ch->d_nstage.ensure(ng), "alloc");
+            opt.nstage = ch->d_nstage.p;
+        }
+        if (want_tr) {
+            CU(ch->d_trace.ensure((size_t)2 * ng * ms), "alloc");
+            CU(cudaMemsetAsync(ch->d_trace.p, 0, (size_t)2 * ng * ms * sizeof(double), cs), "memset");
+            opt.trace_gamma = ch->d_trace.p;
+            opt.trace_inc = ch->d_trace.p + (size_t)ng * ms;
+        }
+        r = nested_batch(ch, ng, ch->d_theta.p, seed, ch->d_streams.p, ch->d_neglog.p, ch->d_status.p, opt);
+        if (r) return ctx->fail(r, ch->err);
+    }
+    std::vector<double> nl, tr;
+    std::vector<int32_t> st, ns;
+    for (Part *p : order) {
+        smcgpu_ctx *ch = p->ch;
+        const int ng = (int)p->idx.size();
+        CU(cudaStreamSynchronize(ch->stream), "sync");
+        nl.resize(ng);
+        st.resize(ng);
+        CU(cudaMemcpy(nl.data(), ch->d_neglog.p, ng * sizeof(double), cudaMemcpyDeviceToHost), "copy");
+        CU(cudaMemcpy(st.data(), ch->d_status.p, ng * sizeof(int32_t), cudaMemcpyDeviceToHost), "copy");
+        if (want_ns) {
+            ns.resize(ng);
+            CU(cudaMemcpy(ns.data(), ch->d_nstage.p, ng * sizeof(int32_t), cudaMemcpyDeviceToHost), "copy");
+        }
+        if (want_tr) {
+            tr.resize((size_t)2 * ng * ms);
+            CU(cudaMemcpy(tr.data(), ch->d_trace.p, tr.size() * sizeof(double), cudaMemcpyDeviceToHost), "copy");
+        }
+        for (int q = 0; q < ng; ++q) {
+            const int i = p->idx[q];
+            neglog[i] = nl[q];
+            status[i] = st[q];
+            if (nstage) nstage[i] = ns[q];
+            if (tg) std::memcpy(tg + (size_t)i * ms, &tr[(size_t)q * ms], ms * sizeof(double));
+            if (ti) std::memcpy(ti + (size_t)i * ms, &tr[(size_t)(ng + q) * ms], ms * sizeof(double));
+        }
+    }
+    if (ctx->stats.on) ctx->stats.evals += n;
     return SMCGPU_OK;
 }
 
@@ -282,6 +420,27 @@ extern "C" int32_t smcgpu_fault_likelihood_batch_dev(smcgpu_ctx *ctx, int32_t n_
         return ctx->fail(SMCGPU_ERR_ARG, "fault_likelihood: bad arguments");
     if (n_theta == 0) return SMCGPU_OK;
     CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+    if (ctx->cfg.patch_km > 0.0) {
+        // per-geometry meshes: the split by mesh is made on the host
+        const int nd = ctx->mesh.ndim_fault;
+        std::vector<double> th((size_t)n_theta * nd), nl(n_theta);
+        std::vector<unsigned long long> sid(n_theta);
+        std::vector<int32_t> st(n_theta);
+        CU(cudaMemcpyAsync(th.data(), theta_dev, th.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+           "copy theta");
+        CU(cudaMemcpyAsync(sid.data(), streams_dev, sid.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                           ctx->stream), "copy streams");
+        CU(cudaStreamSynchronize(ctx->stream), "sync");
+        int r = uneven_eval(ctx, n_theta, th.data(), seed, sid.data(), nl.data(), st.data(), nullptr, nullptr,
+                            nullptr);
+        if (r) return r;
+        CU(cudaMemcpyAsync(neglog_dev, nl.data(), nl.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+           "copy");
+        CU(cudaMemcpyAsync(status_dev, st.data(), st.size() * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream),
+           "copy");
+        CU(cudaStreamSynchronize(ctx->stream), "sync");
+        return SMCGPU_OK;
+    }
     return nested_batch(ctx, n_theta, theta_dev, seed, (const unsigned long long *)streams_dev, neglog_dev,
                         status_dev, NestedOpts());
 }
@@ -295,6 +454,12 @@ static int likelihood_host(smcgpu_ctx *ctx, int n, const double *theta, uint64_t
         return ctx->fail(SMCGPU_ERR_ARG, "fault_likelihood: bad arguments");
     if (n == 0) return SMCGPU_OK;
     CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
+    if (ctx->cfg.patch_km > 0.0) {
+        if (particles_out)
+            return ctx->fail(SMCGPU_ERR_ARG, "the slip population needs a fixed mesh (patch_km = 0)");
+        return uneven_eval(ctx, n, theta, seed, (const unsigned long long *)streams, neglog_out, status_out,
+                           nstage_out, gamma_trace, inc_trace);
+    }
     const int nd = ctx->mesh.ndim_fault, ms = ctx->cfg.max_stages + 2;
     cudaStream_t s = ctx->stream;
     CU(ctx->d_theta.upload(theta, (size_t)n * nd, s), "upload theta");
@@ -537,6 +702,11 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
         }
         std::vector<double> out2(nb);
         std::vector<int32_t> st2(nb), ns2(nb);
+        if (ctx->cfg.patch_km > 0.0) {
+            int rr = uneven_eval(ctx, nb, th2.data(), seed, sid2.data(), out2.data(), st2.data(), ns2.data(), nullptr,
+                                 nullptr);
+            if (rr) return rr;
+        } else {
         CU(d_th.upload(th2.data(), th2.size(), s), "upload");
         CU(d_sid.upload(sid2.data(), sid2.size(), s), "upload");
         CU(d_nl.ensure(nb), "alloc");
@@ -550,6 +720,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
         CU(cudaMemcpyAsync(st2.data(), d_st.p, nb * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
         CU(cudaMemcpyAsync(ns2.data(), d_ns.p, nb * sizeof(int), cudaMemcpyDeviceToHost, s), "copy");
         CU(cudaStreamSynchronize(s), "sync");
+        }
         stv.assign(nb, 0);
         for (int q = 0; q < nb; ++q) {
             out[perm[q]] = out2[q];
@@ -895,6 +1066,7 @@ extern "C" int32_t smcgpu_slip_map(smcgpu_ctx *ctx, int32_t n_theta, const doubl
     if (r) return r;
     if (n_theta < 0 || (n_theta > 0 && (!theta || !streams || !mean_slip_out || !neglog_out || !status_out)))
         return ctx->fail(SMCGPU_ERR_ARG, "slip_map: bad arguments");
+    if (ctx->cfg.patch_km > 0.0) return ctx->fail(SMCGPU_ERR_ARG, "slip_map needs a fixed mesh (patch_km = 0)");
     if (n_theta == 0) return SMCGPU_OK;
     CU(cudaSetDevice(ctx->cfg.device), "cudaSetDevice");
     const int nd = ctx->mesh.ndim_fault, D = ctx->mesh.D;

@@ -18,8 +18,8 @@ bool inner_uses_global(int mixed, int engine, int D) {
 
 const char *inner_size_limit(int mixed, int engine, int D, int N) {
     if (N > 32767) return "nparticle_slip must be < 32768";
-    if (!mixed && D > 512) return "slip dimension too large for the FP64 inner kernel (D <= 512)";
-    if (mixed && D > 1024) return "slip dimension too large for the MIXED inner kernel (D <= 1024)";
+    if (D > 1024) return mixed ? "slip dimension too large for the MIXED inner kernel (D <= 1024)"
+                               : "slip dimension too large for the FP64 inner kernel (D <= 1024)";
     (void)engine;
     return nullptr;
 }
@@ -32,8 +32,8 @@ cudaError_t launch_inner(const MeshDev &m, const InnerArgs &a, cudaStream_t s, c
     if (inner_uses_global(a.mixed, a.engine, D)) {
         if (!a.mgl || !a.glxc) { *why = "inner kernel: global stage-matrix buffers missing"; return cudaErrorInvalidValue; }
         if (!a.mixed) {
-            if (D <= 512) return launch_inner_gl64(m, a, s);
-            *why = "slip dimension too large for the FP64 inner kernel (D <= 512)";
+            if (D <= 1024) return launch_inner_gl64(m, a, s);
+            *why = "slip dimension too large for the FP64 inner kernel (D <= 1024)";
             return cudaErrorInvalidValue;
         }
         if (D <= 1024) return launch_inner_gl32(m, a, s);

@@ -24,7 +24,8 @@ struct InnerArgs {
     float *ll32;          // [th][ll_nnz] FP32 copy of the L^T L values (MIXED), written by the inner kernel
     uint4 *afrag;         // [th][256 * 256 / 4] stage matrix in MMA-fragment order (MIXED, 128 < D <= 256)
     void *mgl;            // global-matrix engine: [th][D][D] stage matrix (float MIXED, double FP64)
-    void *glxc;           // global-matrix engine: [th][16][D] chain states of the slots (same type)
+    void *glxc;           // global-matrix engine: [th][16][D] chain states of the slots (same type; 8 slots
+                          // in FP64 beyond 512 dimensions)
     int *queue;           // device counter of the persistent launch (nullptr: one CTA per G geometries)
     const double *b;      // [th][D]
     const double *dsd;    // [th]
@@ -64,6 +65,6 @@ cudaError_t launch_inner_mma_pair(const MeshDev &m, const InnerArgs &a, cudaStre
 cudaError_t launch_inner_mma_streamed(const MeshDev &m, const InnerArgs &a, cudaStream_t s);          // 128 < D <= 256
 cudaError_t launch_inner_tc(const MeshDev &m, const InnerArgs &a, cudaStream_t s);                    // D <= 128
 cudaError_t launch_inner_gl32(const MeshDev &m, const InnerArgs &a, cudaStream_t s);                  // D <= 1024
-cudaError_t launch_inner_gl64(const MeshDev &m, const InnerArgs &a, cudaStream_t s);                  // D <= 512
+cudaError_t launch_inner_gl64(const MeshDev &m, const InnerArgs &a, cudaStream_t s);                  // D <= 1024
 
 }  // namespace smc

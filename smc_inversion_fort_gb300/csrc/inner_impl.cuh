@@ -431,10 +431,13 @@ struct Layout {
     // in fragment order and streamed through a per-warp ring, and the FP32 Gram
     // matrix of the end-point energies is read from global memory
     static constexpr bool AGL = ENG == ENG_MMA && DP > 128;
-    // global-matrix engine: 16 slots per group of 16 warps; a thread owns
-    // GL_SPT slots of one slot group and DP / (512 * GL_SPT / 16) rows
-    static constexpr int GL_SPT = DP <= 256 ? 8 : 16;
-    static constexpr int S = ENG == ENG_CC ? CW : ENG == ENG_GL ? 16 : (AGL ? 4096 / DP : 2048 / DP);   // slots per warp (CC) / group
+    // global-matrix engine: GL_S slots per group of 16 warps (16; 8 for FP64
+    // beyond 512 dimensions, where a thread's positions, momenta and products
+    // would exceed its registers); a thread owns GL_SPT slots of one slot group
+    // and DP / (512 * GL_SPT / GL_S) rows
+    static constexpr int GL_S = (sizeof(T) == 8 && DP > 512) ? 8 : 16;
+    static constexpr int GL_SPT = DP <= 256 ? 8 : (GL_S == 8 ? 8 : 16);
+    static constexpr int S = ENG == ENG_CC ? CW : ENG == ENG_GL ? GL_S : (AGL ? 4096 / DP : 2048 / DP);   // slots per warp (CC) / group
     static constexpr int RING = 6;                       // streamed k-tiles in flight per warp
     static constexpr uint32_t LBO_A = 2048;              // tcgen05: 128 rows x 16 B per k block
     static constexpr uint32_t LBO_B = 16 * S + 16;       // tcgen05: S rows x 16 B per k block, padded

@@ -2,7 +2,7 @@
 
 This engine keeps the stage matrix M = gamma A + L^T L / alpha^2 of each
 geometry in global memory and streams it once per leapfrog step, so it runs
-any slip dimension up to 1024 (MIXED) or 512 (FP64): the FP64 path above 128
+any slip dimension up to 1024 in both precisions: the FP64 path above 128
 dimensions, the c2 slip size in FP64 and the c4 slip size (32 x 16 patches x
 2 components = 1024).  It is also selectable at any size, which lets its
 FP64 arithmetic be pinned exactly against the oracle on the small cases.
@@ -116,7 +116,7 @@ def test_global_mixed_matches_mma_c0(smcgpu, orc):
     _agree(res[0], res[1])
 
 
-@pytest.mark.parametrize("name", ["d256", "d512"])
+@pytest.mark.parametrize("name", ["d256", "d512", "d1024"])
 def test_fp64_large_d_matches_oracle(smcgpu, orc, name):
     """FP64 above 128 slip dimensions (global-matrix engine) against the
     oracle: -log Z over 16 streams at the true geometry."""
@@ -169,15 +169,11 @@ def test_mixed_large_d_matches_oracle(smcgpu, orc, name):
 
 
 def test_size_limits_are_errors(smcgpu, orc):
-    """Beyond the engine limits the call fails with a clear message, no fallback:
-    FP64 above 512 (17 x 16 patches, D = 544) and MIXED above 1024 (33 x 16)."""
-    w, obs, o = setup_case("d544", orc)
-    g = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
-    g.set_data(obs)
-    with pytest.raises(smcgpu.SmcError, match="D <= 512"):
-        g.fault_calc_likelihood(true_theta(w)[None], 1, np.zeros(1, np.uint64))
+    """Beyond 1024 slip dimensions (33 x 16 patches x 2) the call fails with a
+    clear message in both precisions, before any launch; no fallback."""
     w, obs, o = setup_case("d1056", orc)
-    g = smcgpu.SmcGpu(w.settings, smcgpu.PREC_MIXED)
-    g.set_data(obs)
-    with pytest.raises(smcgpu.SmcError, match="D <= 1024"):
-        g.fault_calc_likelihood(true_theta(w)[None], 1, np.zeros(1, np.uint64))
+    for prec, name in ((smcgpu.PREC_FP64, "FP64"), (smcgpu.PREC_MIXED, "MIXED")):
+        g = smcgpu.SmcGpu(w.settings, prec)
+        g.set_data(obs)
+        with pytest.raises(smcgpu.SmcError, match=f"{name} inner kernel \\(D <= 1024\\)"):
+            g.fault_calc_likelihood(true_theta(w)[None], 1, np.zeros(1, np.uint64))
