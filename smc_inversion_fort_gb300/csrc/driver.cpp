@@ -12,6 +12,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "context.h"
 #include "inner.h"
 
@@ -22,6 +24,13 @@
     } while (0)
 
 namespace {
+
+// NVTX range over a scope (header-only NVTX v3: inert unless a profiler or
+// tracer is attached), named for the stage of the path it covers
+struct Range {
+    explicit Range(const std::string &name) { nvtxRangePushA(name.c_str()); }
+    ~Range() { nvtxRangePop(); }
+};
 
 struct NestedOpts {
     double *trace_gamma = nullptr, *trace_inc = nullptr;  // device, [n][max_stages+2]
@@ -129,6 +138,7 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
     cudaStream_t s = ctx->stream;
     if (const char *why = smc::inner_size_limit(ctx->cfg.precision == SMCGPU_PREC_MIXED, ctx->cfg.inner_engine, D, N))
         return ctx->fail(SMCGPU_ERR_ARG, why);
+    Range range("nested batch: " + std::to_string(n) + " geometries, D = " + std::to_string(D));
     size_t per = bytes_per_theta(ctx);
     size_t budget = (size_t)48 << 30;
     size_t freeb = 0, totb = 0;
@@ -286,6 +296,7 @@ void mesh_of(const smcgpu_ctx *ctx, const double *th, int *nx, int *ne) {
 int uneven_eval(smcgpu_ctx *ctx, int n, const double *theta, uint64_t seed, const unsigned long long *streams,
                 double *neglog, int32_t *status, int32_t *nstage, double *tg, double *ti) {
     const int nd = ctx->mesh.ndim_fault, ms = ctx->cfg.max_stages + 2;
+    Range range("per-geometry meshes: " + std::to_string(n) + " geometries");
     struct Part {
         int nx = 0, ne = 0;
         std::vector<int> idx;
@@ -784,6 +795,7 @@ static int32_t outer_smc(smcgpu_ctx *ctx, const double *range, int32_t N, uint64
     CU(ctx->d_flag.ensure(1), "alloc");
     while (1.0 - gamma > std::pow(10.0, -8.0)) {
         if (ctx->cfg.max_outer_stages != 0 && iter > std::max(ctx->cfg.max_outer_stages, 0)) break;
+        Range stage_range("outer stage " + std::to_string(iter));
         // fault_find_next_gamma (smc_fault.f90:392-485); GSMC tempers L - q
         std::vector<double> nlr(N);
         for (int i = 0; i < N; ++i) nlr[i] = gq ? Ls[i] - qs[i] : Ls[i];
