@@ -45,12 +45,22 @@ def parse():
     p.add_argument("--no-c2", action="store_true", help="skip the c2 (D = 256) nested measurements")
     p.add_argument("--no-c3", action="store_true", help="skip the c3 (per-geometry meshes) nested sample")
     p.add_argument("--no-c4", action="store_true", help="skip the c4 (D = 1024) nested sample")
+    p.add_argument("--c4-full", action="store_true", help="c4: full nested evaluations (about 7.5 minutes)")
     p.add_argument("--fp64-stages", type=int, default=3, help="c0 outer stages timed in FP64")
     p.add_argument("--equal-error-study", type=str, default=None, metavar="OUT_JSON",
                    help="instead of the benchmark: full c0 outer-SMC runs over several seeds in MIXED and FP64 "
                         "(posterior mean / std of every geometry parameter and the evidence), written to OUT_JSON")
     p.add_argument("--study-seeds", type=str, default="8,3", help="MIXED,FP64 seeds of the equal-error study")
     return p.parse_args()
+
+
+_T0 = time.perf_counter()
+PEAKS = {}   # MEASURED_PEAKS.json, loaded by the GPU arm
+
+
+def log(msg: str) -> None:
+    """Progress on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:7.1f} s] {msg}", file=sys.stderr, flush=True)
 
 
 def dist_env():
@@ -252,6 +262,7 @@ def nested_bench(pkg, torch, peaks, fp64_peak, cpu=True, fp64_stages=3):
                        "ntau 50, CV 2 / 0.2", "n_outer": N}
     runs = {}
     for name, prec, k in (("mixed", pkg.PREC_MIXED, 0), ("fp64", pkg.PREC_FP64, fp64_stages)):
+        log(f"c0 outer SMC {name}")
         r = timed_outer_run(pkg, w, obs, rg, prec, 17, k)
         runs[name] = r
         ss = r["stage_s"]
@@ -269,11 +280,13 @@ def nested_bench(pkg, torch, peaks, fp64_peak, cpu=True, fp64_stages=3):
     out["mixed_speedup_vs_fp64"] = {"same_stages": float(runs["fp64"]["stage_s"].sum() / same), "stages": k,
                                     "mixed_all_stages_vs_fp64_first_stages":
                                         out["mixed"]["outer_particles_per_s"] / out["fp64"]["outer_particles_per_s"]}
+    log("c0 equal-error checks")
     out["mixed_vs_fp64"] = equal_error_c0(pkg, w, obs, rg, th_true)
     out["mixed_vs_fp64"]["outer_posterior"] = ("full outer-SMC runs over several seeds in both precisions take "
                                                "about 13 minutes per FP64 run: bench.py --equal-error-study, "
                                                "summarised in profiles/equal_error_c0.md")
     if cpu:
+        log("c0 CPU baseline")
         out["cpu_baseline"] = cpu_nested_rate(w, obs, rg)
         out["mixed_speedup_vs_cpu"] = out["mixed"]["outer_particles_per_s"] / out["cpu_baseline"]["value"]
     return out
@@ -330,15 +343,18 @@ def equal_error_c0(pkg, w, obs, rg, th_true, reps=64, n_prior=16):
     return {"evidence": ev, "slip_posterior_at_truth": slip}
 
 
-def nested_c2_bench(pkg, torch, cpu=True, fp64_sample=152):
+def nested_c2_bench(pkg, torch, cpu=True, fp64_sample=152, sample_stages=2):
     """c2 (16x8 patches x 2 components, D = 256; 400 GNSS stations and 2000
     InSAR points in two paths with a 5 km exponential covariance, 3200
     observations; 2048 inner particles, ntau 50): one outer stage of the
     4096-particle outer SMC in MIXED (timed apart from the initial
-    evaluation), FP64 against MIXED on a sample of prior geometries, and the
-    oracle's per-stage cost on the host cores."""
+    evaluation); FP64 against MIXED on one wave of prior geometries, both
+    stopped after the same first inner stages (a full FP64 evaluation at this
+    size takes about 2.5 minutes of one SM); the oracle's per-stage cost on
+    the host cores."""
     import dataclasses
     w, obs, rg, th_true, s_true = nested_workload(pkg, "c2")
+    log("c2 outer stage (MIXED)")
     r = timed_outer_run(pkg, w, obs, rg, pkg.PREC_MIXED, 19, 1)
     ss = r["stage_s"]
     st = r["stats"]
@@ -353,20 +369,24 @@ def nested_c2_bench(pkg, torch, cpu=True, fp64_sample=152):
     th = random_thetas(w, fp64_sample, seed=12)
     rates = {}
     for name, prec in (("mixed", pkg.PREC_MIXED), ("fp64", pkg.PREC_FP64)):
-        g = pkg.SmcGpu(w.settings, prec)
+        log(f"c2 sample {name}")
+        g = pkg.SmcGpu(dataclasses.replace(w.settings, max_stages=sample_stages), prec)
         g.set_data(obs)
         g.fault_calc_likelihood(th[:2], 5, np.arange(2, dtype=np.uint64))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         nl, stt = g.fault_calc_likelihood(th, 6, np.arange(len(th), dtype=np.uint64) + 100)
         torch.cuda.synchronize()
-        rates[name] = {"nested_evals_per_s": len(th) / (time.perf_counter() - t0), "status_max": int(stt.max()),
-                       "neglog_median": float(np.median(nl))}
+        dt = time.perf_counter() - t0
+        rates[name] = {"geometry_stages_per_s": len(th) * sample_stages / dt, "s_per_batch": dt}
         g.close()
-    out["sample"] = {"geometries": len(th), "note": "one wave of prior geometries (one per SM), both precisions",
+    out["sample"] = {"geometries": len(th), "inner_stages": sample_stages,
+                     "note": "one wave of prior geometries (one per SM), both precisions, each evaluation stopped "
+                             "after the same first inner stages (initial Gibbs population included)",
                      **{k: v for k, v in rates.items()},
-                     "mixed_speedup_vs_fp64": rates["mixed"]["nested_evals_per_s"] / rates["fp64"]["nested_evals_per_s"]}
+                     "mixed_speedup_vs_fp64": rates["fp64"]["s_per_batch"] / rates["mixed"]["s_per_batch"]}
     if cpu:
+        log("c2 CPU baseline")
         out["cpu_baseline"] = cpu_stage_rate(w, obs, th, out["mixed"]["mean_inner_stages"])
         out["mixed_speedup_vs_cpu"] = out["mixed"]["outer_particles_per_s"] / out["cpu_baseline"]["value"]
     return out
@@ -392,13 +412,21 @@ def cpu_stage_rate(w, obs, th, mean_stages, stages=2):
                       f"scaled to the GPU run's mean of {mean_stages:.1f} inner stages per evaluation"}
 
 
-def nested_c4_bench(pkg, torch, sample=152):
+def nested_c4_bench(pkg, torch, sample=152, stages=2):
     """c4 slip size (32x16 patches x 2 components, D = 1024; 400 GNSS and
-    10000 InSAR points in four paths, 11200 observations; 4096 inner
-    particles, ntau 50), MIXED on the global-matrix engine: nested
-    evaluations/s on one wave of prior geometries (one per SM)."""
+    10000 InSAR points in eight paths, 11200 observations; 4096 inner
+    particles, ntau 50), MIXED on the global-matrix engine, one wave of prior
+    geometries (one per SM).  A full evaluation takes about 7.5 minutes at
+    this size, so by default every evaluation stops after `stages` inner
+    stages (stages = 0: full evaluations) and the rate is reported per
+    geometry-stage."""
+    import dataclasses
     from smc_inversion_fort_gb300.configs import random_thetas
+    log("c4 data")
     w, obs, rg, th_true, s_true = nested_workload(pkg, "c4")
+    log("c4 sample")
+    if stages:
+        w = dataclasses.replace(w, settings=dataclasses.replace(w.settings, max_stages=stages))
     g = pkg.SmcGpu(w.settings, pkg.PREC_MIXED)
     g.set_data(obs)
     th = random_thetas(w, sample, seed=13)
@@ -415,15 +443,23 @@ def nested_c4_bench(pkg, torch, sample=152):
     # A once per trajectory end: 4 D^2 (ntau + 2) bytes per trajectory
     traj = st["inner_trajectories"]
     gbs = traj * (w.settings.ntau + 2) * 4.0 * D * D / (st["inner_kernel_ms"] * 1e-3) / 1e9
-    return {"workload": "c4: 32x16 patches (D=1024), 400 GNSS + 10000 InSAR points (11200 obs, 5 km exponential "
-                        "covariance, 4 paths), 4096 inner particles, ntau 50, MIXED",
-            "sample": f"{len(th)} prior geometries in one batch (one per SM)", "s_per_batch": dt,
-            "nested_evals_per_s": len(th) / dt, "outer_particles_per_s": len(th) / dt / 2,
-            "status_max": int(stt.max()), "neglog_median": float(np.median(nl)),
-            "mean_inner_stages": st["inner_stages"] / max(st["nested_evals"], 1),
-            "roofline_inner": {"bound": "hbm", "achieved": gbs, "unit": "GB/s",
-                               "note": "stage matrix (FP32, D^2) streamed per leapfrog step, A per trajectory end",
+    if stt.max() and not stages:
+        log(f"c4: status bits {int(stt.max())}")
+    res = {"workload": "c4: 32x16 patches (D=1024), 400 GNSS + 10000 InSAR points (11200 obs, 5 km exponential "
+                       "covariance, 8 paths), 4096 inner particles, ntau 50, MIXED",
+           "sample": f"{len(th)} prior geometries in one batch (one per SM)" +
+                     (f", every evaluation stopped after {stages} inner stages" if stages else ""),
+           "s_per_batch": dt, "geometry_stages_per_s": st["inner_stages"] / dt,
+           "mean_inner_stages": st["inner_stages"] / max(st["nested_evals"], 1),
+            "roofline_inner": {"bound": "hbm", "achieved": gbs, "peak": PEAKS.get("hbm_gbs"), "unit": "GB/s",
+                               "frac": gbs / PEAKS["hbm_gbs"] if PEAKS.get("hbm_gbs") else None,
+                               "note": "stage matrix (FP32, D^2) streamed per leapfrog step, A per trajectory end; "
+                                       "algorithmic bytes 4 D^2 (ntau + 2) per trajectory",
                                "inner_kernel_s": st["inner_kernel_ms"] * 1e-3}}
+    if not stages:
+        res.update({"nested_evals_per_s": len(th) / dt, "outer_particles_per_s": len(th) / dt / 2,
+                    "status_max": int(stt.max()), "neglog_median": float(np.median(nl))})
+    return res
 
 
 def nested_c3_bench(pkg, torch, sample=304, fp64_sample=152):
@@ -444,6 +480,7 @@ def nested_c3_bench(pkg, torch, sample=304, fp64_sample=152):
            "meshes_in_sample": int(len({mesh_of(w.settings, t) for t in th})),
            "D_min_median_max": [int(D.min()), float(np.median(D)), int(D.max())]}
     for name, prec, n in (("mixed", pkg.PREC_MIXED, sample), ("fp64", pkg.PREC_FP64, fp64_sample)):
+        log(f"c3 sample {name}")
         g = pkg.SmcGpu(w.settings, prec)
         g.set_data(obs)
         g.fault_calc_likelihood(th[:n], 5, np.arange(n, dtype=np.uint64))   # meshes' contexts and buffers
@@ -517,6 +554,7 @@ def gb300_arm(args):
     def step():
         g.greens_dev(n, dth.data_ptr(), out.data_ptr(), pkg.PREC_FP64)
 
+    log("c1 Green's build")
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -553,6 +591,7 @@ def gb300_arm(args):
     if os.path.exists(mp):
         with open(mp) as f:
             peaks = json.load(f)
+    PEAKS.update(peaks)
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     fp64_peak = measured_peak_fp64_tflops(torch, dev)
 
@@ -627,7 +666,7 @@ def gb300_arm(args):
         if not args.no_c3:
             line["nested_smc_c3"] = nested_c3_bench(pkg, torch)
         if not args.no_c4:
-            line["nested_smc_c4"] = nested_c4_bench(pkg, torch)
+            line["nested_smc_c4"] = nested_c4_bench(pkg, torch, stages=0 if args.c4_full else 2)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -663,7 +702,10 @@ def equal_error_study(pkg, torch, args):
     mm, mf = np.array(summ["mixed"]["mean_of_means"]), np.array(summ["fp64"]["mean_of_means"])
     sdm, sdf = np.array(summ["mixed"]["mean_of_stds"]), np.array(summ["fp64"]["mean_of_stds"])
     width = rg[:, 1] - rg[:, 0]
+    log("evidence and slip posterior, 512 streams per geometry")
+    ee = equal_error_c0(pkg, w, obs, rg, th_true, reps=512)
     res = {"workload": "c0 (8x4 patches, D = 64, 60 GNSS stations, 500 outer x 500 inner particles, ntau 50)",
+           "evidence_and_slip": ee,
            "parameters": ["x", "y", "top", "length", "width", "strike", "dip", "log_alpha2"],
            "true_theta": th_true.tolist(), "prior_range": rg.tolist(), "runs": runs, "summary": summ,
            "posterior_mean_rel_diff": ((mm - mf) / np.abs(mf)).tolist(),
