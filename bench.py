@@ -439,10 +439,12 @@ def nested_c4_bench(pkg, torch, sample=152, stages=2):
     st = g.stats()
     g.close()
     D = w.settings.dims()["D"]
-    # the global-matrix engine streams M (D^2 FP32) once per leapfrog step and
-    # A once per trajectory end: 4 D^2 (ntau + 2) bytes per trajectory
+    # the global-matrix engine streams M (D^2 FP32) once per leapfrog step of
+    # a group's 16 chain slots and A once per trajectory end of those slots:
+    # 4 D^2 (ntau + 2) bytes per round of 16 trajectories (slots assumed full,
+    # so the figure is a lower bound on the bytes read)
     traj = st["inner_trajectories"]
-    gbs = traj * (w.settings.ntau + 2) * 4.0 * D * D / (st["inner_kernel_ms"] * 1e-3) / 1e9
+    gbs = traj / 16.0 * (w.settings.ntau + 2) * 4.0 * D * D / (st["inner_kernel_ms"] * 1e-3) / 1e9
     if stt.max() and not stages:
         log(f"c4: status bits {int(stt.max())}")
     res = {"workload": "c4: 32x16 patches (D=1024), 400 GNSS + 10000 InSAR points (11200 obs, 5 km exponential "
@@ -454,7 +456,7 @@ def nested_c4_bench(pkg, torch, sample=152, stages=2):
             "roofline_inner": {"bound": "hbm", "achieved": gbs, "peak": PEAKS.get("hbm_gbs"), "unit": "GB/s",
                                "frac": gbs / PEAKS["hbm_gbs"] if PEAKS.get("hbm_gbs") else None,
                                "note": "stage matrix (FP32, D^2) streamed per leapfrog step, A per trajectory end; "
-                                       "algorithmic bytes 4 D^2 (ntau + 2) per trajectory",
+                                       "algorithmic bytes 4 D^2 (ntau + 2) per round of 16 trajectories (one per chain slot)",
                                "inner_kernel_s": st["inner_kernel_ms"] * 1e-3}}
     if not stages:
         res.update({"nested_evals_per_s": len(th) / dt, "outer_particles_per_s": len(th) / dt / 2,
@@ -462,13 +464,17 @@ def nested_c4_bench(pkg, torch, sample=152, stages=2):
     return res
 
 
-def nested_c3_bench(pkg, torch, sample=304, fp64_sample=152):
+def nested_c3_bench(pkg, torch, sample=304, cmp_sample=152, stages=2, cmp_stages=1):
     """c3: per-geometry meshes (2.5 km patches on a 10-60 km x 5-30 km
     rectangle: 4x2 ... 24x12 patches, D = 16 ... 576) with the c2
     observations and 2048 inner particles, engines from the autotuner's
-    table (SMCGPU_ENGINE_AUTO): nested evaluations/s of one uneven batch of
-    prior geometries in MIXED and FP64 (each call splits the batch by mesh
-    and runs the parts concurrently)."""
+    table (SMCGPU_ENGINE_AUTO).  A full evaluation of the largest meshes takes
+    minutes (FP64: tens of minutes), so every evaluation stops after the same
+    first inner stages: MIXED geometry-stages/s on `sample` prior geometries
+    (each call splits the batch by mesh and runs the parts concurrently), and
+    MIXED against FP64 on the first `cmp_sample` of them, both stopped after
+    `cmp_stages` stages (the initial Gibbs population included)."""
+    import dataclasses
     from smc_inversion_fort_gb300.configs import mesh_of, random_thetas
     w, obs, rg, th_true, s_true = nested_workload(pkg, "c3")
     th = random_thetas(w, sample, seed=14)
@@ -476,26 +482,34 @@ def nested_c3_bench(pkg, torch, sample=304, fp64_sample=152):
     out = {"workload": "c3: 2.5 km patches on 10-60 x 5-30 km rectangles (4x2 ... 24x12 patches, D 16-576), "
                        "400 GNSS + 2000 InSAR points (3200 obs), 2048 inner particles, ntau 50, engines from "
                        "the autotuner's table",
-           "sample": f"{sample} prior geometries (MIXED), the first {fp64_sample} (FP64)",
            "meshes_in_sample": int(len({mesh_of(w.settings, t) for t in th})),
            "D_min_median_max": [int(D.min()), float(np.median(D)), int(D.max())]}
-    for name, prec, n in (("mixed", pkg.PREC_MIXED, sample), ("fp64", pkg.PREC_FP64, fp64_sample)):
-        log(f"c3 sample {name}")
-        g = pkg.SmcGpu(w.settings, prec)
+
+    def run(prec, n, k, seed):
+        g = pkg.SmcGpu(dataclasses.replace(w.settings, max_stages=k), prec)
         g.set_data(obs)
         g.fault_calc_likelihood(th[:n], 5, np.arange(n, dtype=np.uint64))   # meshes' contexts and buffers
         g.stats_reset(True)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        nl, st = g.fault_calc_likelihood(th[:n], 6, np.arange(n, dtype=np.uint64) + 1000)
+        nl, st = g.fault_calc_likelihood(th[:n], seed, np.arange(n, dtype=np.uint64) + 1000)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         stt = g.stats()
         g.close()
-        out[name] = {"nested_evals_per_s": n / dt, "outer_particles_per_s": n / dt / 2, "s_per_batch": dt,
-                     "status_max": int(st.max()), "mean_inner_stages": stt["inner_stages"] / max(stt["nested_evals"], 1)}
-    # the same geometries in both precisions: the FP64 sample's MIXED rate
-    out["mixed_speedup_vs_fp64"] = out["mixed"]["nested_evals_per_s"] / out["fp64"]["nested_evals_per_s"]
+        return {"geometries": n, "inner_stages": k, "s_per_batch": dt,
+                "geometry_stages_per_s": stt["inner_stages"] / dt, "status_max": int(st.max())}
+
+    log("c3 sample mixed")
+    out["mixed"] = run(pkg.PREC_MIXED, sample, stages, 6)
+    out["mixed"]["note"] = f"{sample} prior geometries, every evaluation stopped after {stages} inner stages"
+    cmp = {}
+    for name, prec in (("mixed", pkg.PREC_MIXED), ("fp64", pkg.PREC_FP64)):
+        log(f"c3 comparison {name}")
+        cmp[name] = run(prec, cmp_sample, cmp_stages, 7)
+    out["comparison"] = {"note": f"the first {cmp_sample} geometries in both precisions, every evaluation stopped "
+                                 f"after {cmp_stages} inner stage(s); the largest mesh sets the wall time",
+                         **cmp, "mixed_speedup_vs_fp64": cmp["fp64"]["s_per_batch"] / cmp["mixed"]["s_per_batch"]}
     return out
 
 

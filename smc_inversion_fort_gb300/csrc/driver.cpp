@@ -38,6 +38,10 @@ struct NestedOpts {
     double *particles_out = nullptr;                      // host [N][D] of theta 0 (single-theta call)
     double *lik_out = nullptr, *prior_out = nullptr;      // host [N]
     double *mean_dev = nullptr;                           // device [n][D]: mean final inner population
+    // when set and the batch fits one chunk: stop before the inner SMC launch
+    // and return its arguments here (*deferred = true); the caller launches it
+    smc::InnerArgs *defer = nullptr;
+    bool *deferred = nullptr;
 };
 
 int next_pow2(int n) {
@@ -214,6 +218,11 @@ int nested_batch(smcgpu_ctx *ctx, int n, const double *theta_dev, uint64_t seed,
         smc_resolve_engine(ctx, &a.engine, &a.warps_per_theta);
         a.counters = stats.on ? stats.d_counters.p : nullptr;
         if (ctx->parent && ctx->parent->stats.on) a.counters = ctx->parent->stats.d_counters.p;
+        if (opt.defer && nb == n && !opt.mean_dev && !opt.particles_out && !stats.on) {
+            *opt.defer = a;
+            *opt.deferred = true;
+            return SMCGPU_OK;
+        }
         if (stats.on) CU(stats_mark(stats.inner_ev, s), "stats event");
         cudaError_t e = smc::launch_inner(ctx->md, a, s, &why);
         if (e != cudaSuccess) {
@@ -303,6 +312,15 @@ int uneven_eval(smcgpu_ctx *ctx, int n, const double *theta, uint64_t seed, cons
         std::vector<double> th;
         std::vector<unsigned long long> sid;
         smcgpu_ctx *ch = nullptr;
+        smc::InnerArgs args{};        // the deferred inner launch of this part
+        bool deferred = false;
+        cudaEvent_t ready = nullptr;  // set-up done (then: inner SMC done)
+        Part() = default;
+        Part(const Part &) = delete;
+        Part &operator=(const Part &) = delete;
+        ~Part() {
+            if (ready) cudaEventDestroy(ready);
+        }
     };
     std::map<long long, Part> parts;
     for (int i = 0; i < n; ++i) {
@@ -349,8 +367,54 @@ int uneven_eval(smcgpu_ctx *ctx, int n, const double *theta, uint64_t seed, cons
             opt.trace_gamma = ch->d_trace.p;
             opt.trace_inc = ch->d_trace.p + (size_t)ng * ms;
         }
+        opt.defer = &p->args;
+        opt.deferred = &p->deferred;
         r = nested_batch(ch, ng, ch->d_theta.p, seed, ch->d_streams.p, ch->d_neglog.p, ch->d_status.p, opt);
         if (r) return ctx->fail(r, ch->err);
+        if (p->deferred) {
+            if (!p->ready) CU(cudaEventCreateWithFlags(&p->ready, cudaEventDisableTiming), "event");
+            CU(cudaEventRecord(p->ready, cs), "event");
+        }
+    }
+    // The inner SMC of the deferred parts: parts that run on the same kernel
+    // instantiation (engine, row tile, warps) share one persistent launch, so
+    // the geometries of all their meshes fill the GPU together instead of
+    // one small launch per mesh.  A launch runs on its first part's stream
+    // after every part's set-up, and every part's stream waits for it.
+    {
+        std::map<long long, std::vector<Part *>> groups;
+        for (Part *p : order)
+            if (p->deferred) {
+                const smc::InnerArgs &a = p->args;
+                groups[smc::inner_launch_key(a.mixed, a.engine, a.D, a.warps_per_theta, n)].push_back(p);
+            }
+        for (auto &kv : groups) {
+            std::vector<Part *> &g = kv.second;
+            for (size_t g0 = 0; g0 < g.size(); g0 += smc::INNER_MAX_PARTS) {
+                const size_t g1 = std::min(g.size(), g0 + (size_t)smc::INNER_MAX_PARTS);
+                cudaStream_t ls = g[g0]->ch->stream;
+                static thread_local smc::InnerParts P;   // about 21 KB: kept off the stack
+                P.n = (int)(g1 - g0);
+                P.start[0] = 0;
+                for (size_t q = g0; q < g1; ++q) {
+                    Part *p = g[q];
+                    const int k = (int)(q - g0);
+                    P.m[k] = p->ch->md;
+                    P.a[k] = p->args;
+                    P.start[k + 1] = P.start[k] + p->args.n_theta;
+                    if (p->ch->stream != ls) CU(cudaStreamWaitEvent(ls, p->ready, 0), "wait");
+                }
+                const char *why = nullptr;
+                cudaError_t e = smc::launch_inner_parts(P, ls, &why);
+                if (e != cudaSuccess) {
+                    if (why) return ctx->fail(SMCGPU_ERR_ARG, why);
+                    return ctx->cuda_fail(e, "inner kernel");
+                }
+                Part *lead = g[g0];
+                CU(cudaEventRecord(lead->ready, ls), "event");
+                for (size_t q = g0 + 1; q < g1; ++q) CU(cudaStreamWaitEvent(g[q]->ch->stream, lead->ready, 0), "wait");
+            }
+        }
     }
     std::vector<double> nl, tr;
     std::vector<int32_t> st, ns;

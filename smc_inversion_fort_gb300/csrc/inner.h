@@ -45,6 +45,20 @@ struct InnerArgs {
     unsigned long long *counters;  // optional: [0] += tempering stages, [1] += HMC trajectories
 };
 
+// One inner launch over several parts of a batch: the per-mesh parts of a
+// batch whose geometries carry different meshes (each part with its own mesh
+// tables and buffers).  Part p's geometries are the launch's queue indices
+// start[p] .. start[p+1]-1 (start[0] = 0); the launch takes its configuration
+// and its queue counter from part 0, and every part must map to the same
+// kernel instantiation (inner_launch_key).  A single batch is one part.
+constexpr int INNER_MAX_PARTS = 24;   // keeps the by-value kernel parameters under 32 KB
+struct InnerParts {
+    int n = 0;
+    int start[INNER_MAX_PARTS + 1] = {0};
+    MeshDev m[INNER_MAX_PARTS];
+    InnerArgs a[INNER_MAX_PARTS];
+};
+
 cudaError_t launch_gibbs(const MeshDev &m, const InnerArgs &a, cudaStream_t s);
 // true when a batch of this precision / engine / slip dimension runs on the
 // global-matrix engine (InnerArgs::mgl and ::glxc must then be set)
@@ -52,19 +66,25 @@ bool inner_uses_global(int mixed, int engine, int D);
 // message when no inner engine takes this slip dimension / particle count (else nullptr)
 const char *inner_size_limit(int mixed, int engine, int D, int N);
 cudaError_t launch_inner(const MeshDev &m, const InnerArgs &a, cudaStream_t s, const char **why);
+cudaError_t launch_inner_parts(const InnerParts &P, cudaStream_t s, const char **why);
+// The kernel instantiation (engine family, row tile, warps per geometry) that
+// runs a part of this precision / engine / slip dimension in a launch of
+// n_total geometries: parts with equal keys can share one launch.
+long long inner_launch_key(int mixed, int engine, int D, int warps, int n_total);
 
-// engine families behind launch_inner, one translation unit each
-cudaError_t launch_inner_fp64(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W);           // D <= 128
-cudaError_t launch_inner_fp64_96(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W);        // 64 < D <= 96
-cudaError_t launch_inner_fp64_128(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W);       // 96 < D <= 128
-cudaError_t launch_inner_cc32(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W);           // D <= 192
-cudaError_t launch_inner_cc32_wide(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W);      // 64 < D <= 192
-cudaError_t launch_inner_cc32_192(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W);       // 128 < D <= 192
-cudaError_t launch_inner_mma_wide(const MeshDev &m, const InnerArgs &a, cudaStream_t s);              // D <= 128
-cudaError_t launch_inner_mma_pair(const MeshDev &m, const InnerArgs &a, cudaStream_t s);              // D <= 128
-cudaError_t launch_inner_mma_streamed(const MeshDev &m, const InnerArgs &a, cudaStream_t s);          // 128 < D <= 256
-cudaError_t launch_inner_tc(const MeshDev &m, const InnerArgs &a, cudaStream_t s);                    // D <= 128
-cudaError_t launch_inner_gl32(const MeshDev &m, const InnerArgs &a, cudaStream_t s);                  // D <= 1024
-cudaError_t launch_inner_gl64(const MeshDev &m, const InnerArgs &a, cudaStream_t s);                  // D <= 1024
+// engine families behind launch_inner, one translation unit each; the slip
+// dimension of part 0 picks the row tile (all parts share it)
+cudaError_t launch_inner_fp64(const InnerParts &P, cudaStream_t s, int W);           // D <= 128
+cudaError_t launch_inner_fp64_96(const InnerParts &P, cudaStream_t s, int W);        // 64 < D <= 96
+cudaError_t launch_inner_fp64_128(const InnerParts &P, cudaStream_t s, int W);       // 96 < D <= 128
+cudaError_t launch_inner_cc32(const InnerParts &P, cudaStream_t s, int W);           // D <= 192
+cudaError_t launch_inner_cc32_wide(const InnerParts &P, cudaStream_t s, int W);      // 64 < D <= 192
+cudaError_t launch_inner_cc32_192(const InnerParts &P, cudaStream_t s, int W);       // 128 < D <= 192
+cudaError_t launch_inner_mma_wide(const InnerParts &P, cudaStream_t s);              // D <= 128
+cudaError_t launch_inner_mma_pair(const InnerParts &P, cudaStream_t s);              // D <= 128
+cudaError_t launch_inner_mma_streamed(const InnerParts &P, cudaStream_t s);          // 128 < D <= 256
+cudaError_t launch_inner_tc(const InnerParts &P, cudaStream_t s);                    // D <= 128
+cudaError_t launch_inner_gl32(const InnerParts &P, cudaStream_t s);                  // D <= 1024
+cudaError_t launch_inner_gl64(const InnerParts &P, cudaStream_t s);                  // D <= 1024
 
 }  // namespace smc

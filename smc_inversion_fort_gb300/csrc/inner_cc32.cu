@@ -4,11 +4,11 @@
 
 namespace smc {
 
-cudaError_t launch_inner_cc32(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W) {
-    const int D = a.D;
-    if (D <= 32) return launch_cc_t<float, 2>(m, a, s, W);
-    if (D <= 64) return launch_cc_t<float, 4>(m, a, s, W);
-    return launch_inner_cc32_wide(m, a, s, W);
+cudaError_t launch_inner_cc32(const InnerParts &P, cudaStream_t s, int W) {
+    const int D = P.a[0].D;
+    if (D <= 32) return launch_cc_t<float, 2>(P, s, W);
+    if (D <= 64) return launch_cc_t<float, 4>(P, s, W);
+    return launch_inner_cc32_wide(P, s, W);
 }
 
 }  // namespace smc

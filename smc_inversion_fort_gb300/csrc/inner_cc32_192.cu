@@ -3,8 +3,8 @@
 
 namespace smc {
 
-cudaError_t launch_inner_cc32_192(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W) {
-    return launch_cc_t<float, 12>(m, a, s, W);
+cudaError_t launch_inner_cc32_192(const InnerParts &P, cudaStream_t s, int W) {
+    return launch_cc_t<float, 12>(P, s, W);
 }
 
 }  // namespace smc

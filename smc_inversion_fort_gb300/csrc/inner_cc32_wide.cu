@@ -4,11 +4,11 @@
 
 namespace smc {
 
-cudaError_t launch_inner_cc32_wide(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W) {
-    const int D = a.D;
-    if (D <= 96) return launch_cc_t<float, 6>(m, a, s, W);
-    if (D <= 128) return launch_cc_t<float, 8>(m, a, s, W);
-    return launch_inner_cc32_192(m, a, s, W);
+cudaError_t launch_inner_cc32_wide(const InnerParts &P, cudaStream_t s, int W) {
+    const int D = P.a[0].D;
+    if (D <= 96) return launch_cc_t<float, 6>(P, s, W);
+    if (D <= 128) return launch_cc_t<float, 8>(P, s, W);
+    return launch_inner_cc32_192(P, s, W);
 }
 
 }  // namespace smc

@@ -4,12 +4,12 @@
 
 namespace smc {
 
-cudaError_t launch_inner_fp64(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W) {
-    const int D = a.D;
-    if (D <= 32) return launch_cc_t<double, 2>(m, a, s, W);
-    if (D <= 64) return launch_cc_t<double, 4>(m, a, s, W);
-    if (D <= 96) return launch_inner_fp64_96(m, a, s, W);
-    return launch_inner_fp64_128(m, a, s, W);
+cudaError_t launch_inner_fp64(const InnerParts &P, cudaStream_t s, int W) {
+    const int D = P.a[0].D;
+    if (D <= 32) return launch_cc_t<double, 2>(P, s, W);
+    if (D <= 64) return launch_cc_t<double, 4>(P, s, W);
+    if (D <= 96) return launch_inner_fp64_96(P, s, W);
+    return launch_inner_fp64_128(P, s, W);
 }
 
 }  // namespace smc

@@ -3,8 +3,8 @@
 
 namespace smc {
 
-cudaError_t launch_inner_fp64_96(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W) {
-    return launch_cc_t<double, 6>(m, a, s, W);
+cudaError_t launch_inner_fp64_96(const InnerParts &P, cudaStream_t s, int W) {
+    return launch_cc_t<double, 6>(P, s, W);
 }
 
 }  // namespace smc

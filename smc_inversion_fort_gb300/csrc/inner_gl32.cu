@@ -4,10 +4,10 @@
 
 namespace smc {
 
-cudaError_t launch_inner_gl32(const MeshDev &m, const InnerArgs &a, cudaStream_t s) {
-    if (a.D <= 256) return launch_gl_t<float, 16>(m, a, s);
-    if (a.D <= 512) return launch_gl_t<float, 32>(m, a, s);
-    return launch_gl_t<float, 64>(m, a, s);
+cudaError_t launch_inner_gl32(const InnerParts &P, cudaStream_t s) {
+    if (P.a[0].D <= 256) return launch_gl_t<float, 16>(P, s);
+    if (P.a[0].D <= 512) return launch_gl_t<float, 32>(P, s);
+    return launch_gl_t<float, 64>(P, s);
 }
 
 }  // namespace smc

@@ -231,13 +231,38 @@ __device__ __forceinline__ double wreduce_n(double v[NV], int lane) {
     return t;
 }
 
+// 4- or 8-byte asynchronous global -> shared copy (through L1), in commit groups
+template <int BYTES>
+__device__ __forceinline__ void cp_async_small(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(tc::smem_u32(dst)), "l"(src), "n"(BYTES)
+                 : "memory");
+}
+// (d0, d1) += a * (b0, b1) as one packed FP32x2 FMA: each lane is an FP32 fma,
+// rounded as fmaf
+__device__ __forceinline__ void ffma2(float &d0, float &d1, float a, float b0, float b1) {
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
+        "mov.b64 pa, {%2, %2};\n\t"
+        "mov.b64 pb, {%3, %4};\n\t"
+        "mov.b64 pd, {%0, %1};\n\t"
+        "fma.rn.f32x2 pd, pa, pb, pd;\n\t"
+        "mov.b64 {%0, %1}, pd;\n\t}"
+        : "+f"(d0), "+f"(d1)
+        : "f"(a), "f"(b0), "f"(b1));
+}
+
 // Global-matrix step product: acc[i][s] = sum_k Mg[k][r_i] X[k][s0 + s] for the
 // thread's rows r_i = row0 + i * RP (column-major Mg with leading dimension
-// D, read through L1/L2 with plain loads: the matrix is rewritten every
-// stage) and its SPT slots of the shared operand X (row stride S).
-template <typename T, int R, int SPT, int RP, int S>
+// D; the matrix is rewritten every stage) and its SPT slots of the shared
+// operand X (row stride S).  Each element of Mg is used by one thread only, so
+// every thread streams its own R entries of the columns k + 1 .. k + P - 1
+// through a private ring of P column slots in shared memory (ring[(slot R + i)
+// * NTH + tid]) with cp.async while it multiplies column k: a column needs a
+// cp.async.wait_group and no barrier, and P columns of every thread are in
+// flight instead of one blocking load.  A ring slot is refilled only after the
+// thread's own read of it fed its FMAs.  Results equal the plain loop's.
+template <typename T, int R, int SPT, int RP, int S, int P, int NTH>
 __device__ __forceinline__ void gl_gemm(const T *Mg, int D, const T *__restrict__ X, int row0, int s0,
-                                        T acc[R][SPT]) {
+                                        T *ring, int tid, T acc[R][SPT]) {
 #pragma unroll
     for (int i = 0; i < R; ++i)
 #pragma unroll
@@ -245,11 +270,26 @@ __device__ __forceinline__ void gl_gemm(const T *Mg, int D, const T *__restrict_
     bool live[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) live[i] = row0 + i * RP < D;
-#pragma unroll 4
+    T *my = ring + tid;
+    auto issue = [&](int k, int slot) {
+        if (k < D) {
+            const T *src = Mg + (size_t)k * D + row0;
+#pragma unroll
+            for (int i = 0; i < R; ++i)
+                if (live[i]) cp_async_small<sizeof(T)>(my + (slot * R + i) * NTH, src + i * RP);
+        }
+        cp_async_commit();   // empty groups past the last column keep the count uniform
+    };
+#pragma unroll
+    for (int kk = 0; kk < P; ++kk) issue(kk, kk);
+    int slot = 0;
+#pragma unroll 2
     for (int k = 0; k < D; ++k) {
+        // groups committed: columns 0 .. k + P - 1; at most P - 1 pending means column k has landed
+        cp_async_wait<P - 1>();
         T mv[R];
 #pragma unroll
-        for (int i = 0; i < R; ++i) mv[i] = live[i] ? Mg[(size_t)k * D + row0 + i * RP] : T(0);
+        for (int i = 0; i < R; ++i) mv[i] = live[i] ? my[(slot * R + i) * NTH] : T(0);
         const T *xk = X + k * S + s0;   // 16-byte aligned: S and s0 are multiples of 8
         if constexpr (sizeof(T) == 4) {
 #pragma unroll
@@ -257,10 +297,8 @@ __device__ __forceinline__ void gl_gemm(const T *Mg, int D, const T *__restrict_
                 const float4 v = *reinterpret_cast<const float4 *>(xk + q);
 #pragma unroll
                 for (int i = 0; i < R; ++i) {
-                    acc[i][q] = fmaf((float)mv[i], v.x, (float)acc[i][q]);
-                    acc[i][q + 1] = fmaf((float)mv[i], v.y, (float)acc[i][q + 1]);
-                    acc[i][q + 2] = fmaf((float)mv[i], v.z, (float)acc[i][q + 2]);
-                    acc[i][q + 3] = fmaf((float)mv[i], v.w, (float)acc[i][q + 3]);
+                    ffma2(acc[i][q], acc[i][q + 1], (float)mv[i], v.x, v.y);
+                    ffma2(acc[i][q + 2], acc[i][q + 3], (float)mv[i], v.z, v.w);
                 }
             }
         } else {
@@ -274,6 +312,8 @@ __device__ __forceinline__ void gl_gemm(const T *Mg, int D, const T *__restrict_
                 }
             }
         }
+        issue(k + P, slot);   // column k + P into the slot just consumed
+        slot = slot + 1 == P ? 0 : slot + 1;
     }
 }
 
@@ -437,6 +477,11 @@ struct Layout {
     // and DP / (512 * GL_SPT / GL_S) rows
     static constexpr int GL_S = (sizeof(T) == 8 && DP > 512) ? 8 : 16;
     static constexpr int GL_SPT = DP <= 256 ? 8 : (GL_S == 8 ? 8 : 16);
+    // columns of the stage matrix in flight per thread (gl_gemm's ring): a
+    // ring slot holds the thread's DP / RP entries of one column, and the
+    // ring of the whole group takes GL_RING * DP * (GL_S / GL_SPT) entries
+    static constexpr int GL_RING = (sizeof(T) == 8 && DP > 512) ? 6 : 16;
+    static constexpr size_t GL_RING_BYTES = (size_t)GL_RING * DP * (GL_S / GL_SPT) * sizeof(T);
     static constexpr int S = ENG == ENG_CC ? CW : ENG == ENG_GL ? GL_S : (AGL ? 4096 / DP : 2048 / DP);   // slots per warp (CC) / group
     static constexpr int RING = 6;                       // streamed k-tiles in flight per warp
     static constexpr uint32_t LBO_A = 2048;              // tcgen05: 128 rows x 16 B per k block
@@ -454,7 +499,7 @@ struct Layout {
         return AGL ? (size_t)W * RING * mtiles_per_warp(W) * 2 * 32 * 16 : 0;
     }
     __host__ __device__ static size_t engine_bytes(int W) {
-        if (ENG == ENG_GL) return (size_t)DP * S * sizeof(T);  // the step operand [row][slot]
+        if (ENG == ENG_GL) return (size_t)DP * S * sizeof(T) + GL_RING_BYTES;  // step operand [row][slot], ring
         if (ENG == ENG_TC) return 2 * A_BYTES + 2 * B_BYTES;   // the end-point tile Xf aliases B
         if (ENG == ENG_MMA)   // + the FP32 Gram matrix for the end-point energies (or the A ring)
             return 2 * A_BYTES + 4 * B_BYTES + 3 * TILE_BYTES +
@@ -510,7 +555,8 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
         static_assert(2 * L_::B_BYTES >= L_::TILE_BYTES, "offset tile must fit in one B buffer");
     } else if constexpr (ENG == ENG_GL) {
         Msm = nullptr;
-        Xw0 = (T *)sp;   // step operand [row][slot]
+        Xw0 = (T *)sp;                        // step operand [row][slot]
+        Xw1 = Xw0 + (size_t)DP * L_::S;       // gl_gemm's per-thread column ring
     } else if constexpr (TC) {
         Ahi = sp; Alo = Ahi + L_::A_BYTES; Bhi = Alo + L_::A_BYTES; Blo = Bhi + L_::B_BYTES;
         Xf = (float *)Bhi;   // written at the last leapfrog step, after the last MMA read B
@@ -1546,7 +1592,7 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                         write_x(x, actm);
                         grp.sync();
                         T acc[R][SPT];
-                        gl_gemm<T, R, SPT, RP, S>(Mg, D, Xs, row0, s0, acc);
+                        gl_gemm<T, R, SPT, RP, S, L_::GL_RING, NTH>(Mg, D, Xs, row0, s0, Xw1, gt, acc);
                         grp.sync();
                         const unsigned blm = m32[4];
                         const T hs = it == 0 ? T(0.5) : T(1), xs = it == a.ntau ? T(0.5) : T(1);
@@ -1576,8 +1622,8 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                     grp.sync();
                     const unsigned blm = m32[4];
                     T af[R][SPT];
-                    if constexpr (MIXED) gl_gemm<T, R, SPT, RP, S>((const T *)A32, D, Xs, row0, s0, af);
-                    else gl_gemm<T, R, SPT, RP, S>((const T *)Ath, D, Xs, row0, s0, af);
+                    if constexpr (MIXED) gl_gemm<T, R, SPT, RP, S, L_::GL_RING, NTH>((const T *)A32, D, Xs, row0, s0, Xw1, gt, af);
+                    else gl_gemm<T, R, SPT, RP, S, L_::GL_RING, NTH>((const T *)Ath, D, Xs, row0, s0, Xw1, gt, af);
                     // per-slot sums over the thread's rows, one quantity at a time
                     double v[SPT];
                     // likelihood term (MIXED: g.delta + delta.A delta / 2; FP64: x.A x - 2 b.x)
@@ -2255,7 +2301,7 @@ __host__ __device__ constexpr uint32_t tmem_columns(int n) {
 }
 
 template <typename T, int RT, int ENG, int WG>
-__device__ __forceinline__ void inner_group_entry(const MeshDev &m, const InnerArgs &a, int W, int G) {
+__device__ __forceinline__ void inner_group_entry(const InnerParts &P, int W, int G) {
     extern __shared__ __align__(128) unsigned char smem_all[];
     __shared__ uint32_t tmem_slot;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -2282,23 +2328,31 @@ __device__ __forceinline__ void inner_group_entry(const MeshDev &m, const InnerA
     }
     if (grp.id < G) {
         unsigned char *gsm = smem_all + (size_t)grp.id * Layout<T, RT, ENG>::bytes(W);
-        if (ENG == ENG_TC || !a.queue) {
-            const int th = blockIdx.x * G + grp.id;
-            if (th < a.n_theta) group_body<T, RT, ENG, WG>(m, a, grp, th, gsm, tmem_base);
-        } else {
-            // persistent groups: a group takes the next geometry from the
-            // queue when it finishes one, so uneven geometries balance at the
-            // granularity of one geometry (not of a CTA's G geometries)
-            __shared__ int next_th[8];
-            while (true) {
-                if (grp.gt == 0) next_th[grp.id] = atomicAdd(a.queue, 1);
+        const int ntot = P.start[P.n];
+        int *queue = P.a[0].queue;
+        // persistent groups (with a queue): a group takes the next geometry
+        // from the queue when it finishes one, so uneven geometries balance at
+        // the granularity of one geometry (not of a CTA's G geometries);
+        // without a queue (and always for tcgen05), one geometry per group
+        const bool persistent = ENG != ENG_TC && queue != nullptr;
+        __shared__ int next_th[8];
+        for (int round = 0;; ++round) {
+            int th;
+            if (persistent) {
+                if (grp.gt == 0) next_th[grp.id] = atomicAdd(queue, 1);
                 grp.sync();
-                const int th = next_th[grp.id];
+                th = next_th[grp.id];
                 grp.sync();
-                if (th >= a.n_theta) break;
-                group_body<T, RT, ENG, WG>(m, a, grp, th, gsm, tmem_base);
-                grp.sync();
+            } else {
+                if (round > 0) break;
+                th = blockIdx.x * G + grp.id;
             }
+            if (th >= ntot) break;
+            // the part that holds queue index th (parts are few: a linear scan)
+            int p = 0;
+            while (p + 1 < P.n && th >= P.start[p + 1]) ++p;
+            group_body<T, RT, ENG, WG>(P.m[p], P.a[p], grp, th - P.start[p], gsm, tmem_base);
+            grp.sync();
         }
     }
     if constexpr (ENG == ENG_TC) {
@@ -2310,40 +2364,43 @@ __device__ __forceinline__ void inner_group_entry(const MeshDev &m, const InnerA
 }
 
 template <typename T, int RT, int ENG, int WG>
-__global__ void __launch_bounds__(ENG == ENG_MMA ? 512 : 256) inner_group_kernel(MeshDev m, InnerArgs a, int W, int G) {
-    inner_group_entry<T, RT, ENG, WG>(m, a, W, G);
+__global__ void __launch_bounds__(ENG == ENG_MMA ? 512 : 256) inner_group_kernel(const __grid_constant__ InnerParts P,
+                                                                               int W, int G) {
+    inner_group_entry<T, RT, ENG, WG>(P, W, G);
 }
 
 // the global-matrix engine: one 512-thread CTA per SM, so up to 128 registers
 // per thread for the positions, momenta and products of its rows and slots
 template <typename T, int RT>
-__global__ void __launch_bounds__(512, 1) inner_gl_kernel(MeshDev m, InnerArgs a) {
-    inner_group_entry<T, RT, ENG_GL, 16>(m, a, 16, 1);
+__global__ void __launch_bounds__(512, 1) inner_gl_kernel(const __grid_constant__ InnerParts P) {
+    inner_group_entry<T, RT, ENG_GL, 16>(P, 16, 1);
 }
 
 // CTAs of a persistent launch: one wave (resident CTAs), no more than the
 // geometries need; the queue counter is reset on the launch's stream.
 // Without a queue, one CTA per G geometries.
-static unsigned persistent_blocks(const InnerArgs &a, int G, int resident, cudaStream_t s) {
-    const int need = (a.n_theta + G - 1) / G;
-    if (!a.queue) return (unsigned)need;
-    if (cudaMemsetAsync(a.queue, 0, sizeof(int), s) != cudaSuccess) return 0;
+static unsigned persistent_blocks(const InnerParts &P, int G, int resident, cudaStream_t s) {
+    const int need = (P.start[P.n] + G - 1) / G;
+    int *queue = P.a[0].queue;
+    if (!queue) return (unsigned)need;
+    if (cudaMemsetAsync(queue, 0, sizeof(int), s) != cudaSuccess) return 0;
     return (unsigned)std::max(1, std::min(need, resident));
 }
 
 template <typename T, int RT>
-static cudaError_t launch_cc_t(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int W) {
+static cudaError_t launch_cc_t(const InnerParts &P, cudaStream_t s, int W) {
     using L_ = Layout<T, RT, ENG_CC>;
     int dev = 0, maxsm = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int ntot = P.start[P.n];
     if (W <= 0) {
         // warps per geometry from the batch size: enough geometries in flight
         // to fill every SM with 8 warps, otherwise more slots per geometry
         const long long slots = 8LL * nsm;
         W = 1;
-        while (W < 8 && (long long)a.n_theta * W * 2 <= slots) W *= 2;
+        while (W < 8 && (long long)ntot * W * 2 <= slots) W *= 2;
     }
     size_t per = L_::bytes(W);
     int G = (int)std::min<size_t>((size_t)(8 / W), (size_t)maxsm / per);
@@ -2360,49 +2417,54 @@ static cudaError_t launch_cc_t(const MeshDev &m, const InnerArgs &a, cudaStream_
     int occ = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, inner_group_kernel<T, RT, ENG_CC, 0>, 32 * W * G, sm);
     if (e != cudaSuccess) return e;
-    const unsigned blocks = persistent_blocks(a, G, nsm * std::max(occ, 1), s);
+    const unsigned blocks = persistent_blocks(P, G, nsm * std::max(occ, 1), s);
     if (!blocks) return cudaGetLastError();
-    inner_group_kernel<T, RT, ENG_CC, 0><<<blocks, 32 * W * G, sm, s>>>(m, a, W, G);
+    inner_group_kernel<T, RT, ENG_CC, 0><<<blocks, 32 * W * G, sm, s>>>(P, W, G);
     return cudaGetLastError();
 }
 
 // WG warps per geometry: as many geometries per CTA as shared memory and the
 // register file allow (gmax), but no more than needed to give every SM a CTA
 template <int RT, int ENG, int WG>
-static cudaError_t launch_wg_t(const MeshDev &m, const InnerArgs &a, cudaStream_t s, int gmax) {
+static cudaError_t launch_wg_t(const InnerParts &P, cudaStream_t s, int gmax) {
     using L_ = Layout<float, RT, ENG>;
     int dev = 0, maxsm = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int ntot = P.start[P.n];
     const size_t per = L_::bytes(WG);
     int G = (int)std::min<size_t>((size_t)gmax, (size_t)maxsm / per);
-    G = std::min(G, std::max(1, (a.n_theta + nsm - 1) / nsm));
+    G = std::min(G, std::max(1, (ntot + nsm - 1) / nsm));
     if (G < 1) return cudaErrorInvalidValue;
     const size_t sm = per * G;
     cudaError_t e = cudaFuncSetAttribute(inner_group_kernel<float, RT, ENG, WG>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    unsigned blocks = (unsigned)((a.n_theta + G - 1) / G);
+    unsigned blocks = (unsigned)((ntot + G - 1) / G);
     if (ENG != ENG_TC) {
         int occ = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, inner_group_kernel<float, RT, ENG, WG>, 32 * WG * G, sm);
         if (e != cudaSuccess) return e;
-        blocks = persistent_blocks(a, G, nsm * std::max(occ, 1), s);
+        blocks = persistent_blocks(P, G, nsm * std::max(occ, 1), s);
         if (!blocks) return cudaGetLastError();
     }
-    inner_group_kernel<float, RT, ENG, WG><<<blocks, 32 * WG * G, sm, s>>>(m, a, WG, G);
+    inner_group_kernel<float, RT, ENG, WG><<<blocks, 32 * WG * G, sm, s>>>(P, WG, G);
     return cudaGetLastError();
 }
 
 // Global-matrix engine: one geometry per CTA of 16 warps, persistent over the
 // batch (a CTA takes the next geometry from the queue when it finishes one).
 template <typename T, int RT>
-static cudaError_t launch_gl_t(const MeshDev &m, const InnerArgs &a, cudaStream_t s) {
+static cudaError_t launch_gl_t(const InnerParts &P, cudaStream_t s) {
     using L_ = Layout<T, RT, ENG_GL>;
     constexpr int WG = 16;
-    if (a.D > L_::DP || !a.mgl || !a.glxc || !a.queue) return cudaErrorInvalidValue;
-    if (!std::is_same<T, double>::value && !a.A32) return cudaErrorInvalidValue;
+    for (int p = 0; p < P.n; ++p) {
+        const InnerArgs &a = P.a[p];
+        if (a.D > L_::DP || !a.mgl || !a.glxc) return cudaErrorInvalidValue;
+        if (!std::is_same<T, double>::value && !a.A32) return cudaErrorInvalidValue;
+    }
+    if (!P.a[0].queue) return cudaErrorInvalidValue;
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -2413,9 +2475,9 @@ static cudaError_t launch_gl_t(const MeshDev &m, const InnerArgs &a, cudaStream_
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, inner_gl_kernel<T, RT>, 32 * WG, sm);
     if (e != cudaSuccess) return e;
     if (occ < 1) return cudaErrorInvalidConfiguration;
-    const unsigned blocks = persistent_blocks(a, 1, nsm * occ, s);
+    const unsigned blocks = persistent_blocks(P, 1, nsm * occ, s);
     if (!blocks) return cudaGetLastError();
-    inner_gl_kernel<T, RT><<<blocks, 32 * WG, sm, s>>>(m, a);
+    inner_gl_kernel<T, RT><<<blocks, 32 * WG, sm, s>>>(P);
     return cudaGetLastError();
 }
 

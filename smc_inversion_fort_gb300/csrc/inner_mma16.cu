@@ -4,11 +4,11 @@
 
 namespace smc {
 
-cudaError_t launch_inner_mma_wide(const MeshDev &m, const InnerArgs &a, cudaStream_t s) {
-    const int D = a.D;
-    if (D <= 32) return launch_wg_t<2, ENG_MMA, 16>(m, a, s, 1);
-    if (D <= 64) return launch_wg_t<4, ENG_MMA, 16>(m, a, s, 1);
-    return launch_wg_t<8, ENG_MMA, 16>(m, a, s, 1);
+cudaError_t launch_inner_mma_wide(const InnerParts &P, cudaStream_t s) {
+    const int D = P.a[0].D;
+    if (D <= 32) return launch_wg_t<2, ENG_MMA, 16>(P, s, 1);
+    if (D <= 64) return launch_wg_t<4, ENG_MMA, 16>(P, s, 1);
+    return launch_wg_t<8, ENG_MMA, 16>(P, s, 1);
 }
 
 }  // namespace smc

@@ -4,8 +4,8 @@
 
 namespace smc {
 
-cudaError_t launch_inner_mma_streamed(const MeshDev &m, const InnerArgs &a, cudaStream_t s) {
-    return launch_wg_t<16, ENG_MMA, 16>(m, a, s, 1);
+cudaError_t launch_inner_mma_streamed(const InnerParts &P, cudaStream_t s) {
+    return launch_wg_t<16, ENG_MMA, 16>(P, s, 1);
 }
 
 }  // namespace smc

@@ -4,11 +4,11 @@
 
 namespace smc {
 
-cudaError_t launch_inner_mma_pair(const MeshDev &m, const InnerArgs &a, cudaStream_t s) {
-    const int D = a.D;
-    if (D <= 32) return launch_wg_t<2, ENG_MMA, 8>(m, a, s, 2);
-    if (D <= 64) return launch_wg_t<4, ENG_MMA, 8>(m, a, s, 2);
-    return launch_wg_t<8, ENG_MMA, 8>(m, a, s, 2);
+cudaError_t launch_inner_mma_pair(const InnerParts &P, cudaStream_t s) {
+    const int D = P.a[0].D;
+    if (D <= 32) return launch_wg_t<2, ENG_MMA, 8>(P, s, 2);
+    if (D <= 64) return launch_wg_t<4, ENG_MMA, 8>(P, s, 2);
+    return launch_wg_t<8, ENG_MMA, 8>(P, s, 2);
 }
 
 }  // namespace smc

@@ -141,6 +141,52 @@ def test_nested_fp64_statistics_match_oracle(smcgpu, orc):
     assert abs(a.mean() - b.mean()) < 4 * se + 1e-6
 
 
+def test_nested_fp64_statistics_match_oracle_c0(smcgpu, orc):
+    """The c0 workload (8x4 patches x 2 components = 64 slip parameters, 60
+    GNSS stations, 500 inner particles, ntau 50) in FP64 against the oracle:
+    at the true geometry and at two prior-box geometries, the mean and the
+    median -log Z over 32 independent streams agree within 4 standard
+    errors."""
+    w, obs, o = setup_case("c0", orc)
+    th = np.vstack([true_theta(w)[None], random_thetas(w, 2, seed=11)])
+    reps = 32
+    thr = np.repeat(th, reps, axis=0)
+    streams = np.arange(len(thr), dtype=np.uint64) + 8100
+    g = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
+    g.set_data(obs)
+    a, sa = g.fault_calc_likelihood(thr, 37, streams)
+    b, sb = o.fault_likelihood_batch(thr, 37, streams + 10**6)
+    assert np.all(sa == 0) and np.all(sb == 0)
+    a, b = a.reshape(-1, reps), b.reshape(-1, reps)
+    se = np.sqrt((a.var(1, ddof=1) + b.var(1, ddof=1)) / reps)
+    print("gpu   ", a.mean(1), np.median(a, 1), "\noracle", b.mean(1), np.median(b, 1), "\nse    ", se)
+    assert np.all(np.abs(a.mean(1) - b.mean(1)) < 4 * se + 1e-9)
+    assert np.all(np.abs(np.median(a, 1) - np.median(b, 1)) < 4 * 1.2533 * se + 1e-9)
+
+
+def test_posterior_population_c0(smcgpu, orc):
+    """The c0 slip posterior (final inner population at the true geometry) in
+    FP64 against the oracle: per-component posterior means over 8 independent
+    streams within 4 standard errors (+1 mm)."""
+    w, obs, o = setup_case("c0", orc)
+    th = true_theta(w)
+    g = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
+    g.set_data(obs)
+    n = 8
+    mg, mr = [], []
+    for k in range(n):
+        got = g.fault_likelihood_posterior(th, 6, 300 + k)
+        ref = o.fault_likelihood(th, 6, 10**6 + 300 + k)
+        assert got["status"] == 0 and ref["status"] == 0
+        mg.append(got["particles"].mean(0))
+        mr.append(ref["particles"].mean(0))
+    mg, mr = np.array(mg), np.array(mr)
+    se = np.sqrt((mg.var(0, ddof=1) + mr.var(0, ddof=1)) / n)
+    diff = np.abs(mg.mean(0) - mr.mean(0))
+    print("max |diff|", diff.max(), "max se", se.max(), "peak mean slip", mr.mean(0).max())
+    assert np.all(diff <= 4 * se + 1e-3)
+
+
 @pytest.mark.parametrize("engine", ["mma", "cuda", "tcgen05"])
 def test_nested_mixed_matches_fp64(smcgpu, orc, engine):
     """MIXED against FP64, for every leapfrog engine (warp-level BF16x3 MMA,
