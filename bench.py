@@ -51,6 +51,13 @@ def parse():
                    help="instead of the benchmark: full c0 outer-SMC runs over several seeds in MIXED and FP64 "
                         "(posterior mean / std of every geometry parameter and the evidence), written to OUT_JSON")
     p.add_argument("--study-seeds", type=str, default="8,3", help="MIXED,FP64 seeds of the equal-error study")
+    p.add_argument("--study-seed0", type=str, default="1000,1000",
+                   help="equal-error study: MIXED,FP64 seed offsets (seeds are offset + 1, offset + 2, ...)")
+    p.add_argument("--equal-error-points", type=str, default=None, metavar="THETAS",
+                   help="c0: -log Z in MIXED and FP64 over 512 streams at the given geometries "
+                        "('x,y,top,length,width,strike,dip,log_alpha2;...')")
+    p.add_argument("--study-no-evidence", action="store_true",
+                   help="equal-error study: only the outer-SMC runs (no 512-stream evidence comparison)")
     return p.parse_args()
 
 
@@ -551,6 +558,9 @@ def gb300_arm(args):
     if args.equal_error_study:
         equal_error_study(pkg, torch, args)
         return
+    if args.equal_error_points:
+        equal_error_points(pkg, args.equal_error_points)
+        return
     w, obs, th = workload(args.n_theta)
     g = pkg.SmcGpu(w.settings, device=local)
     g.set_data(obs)
@@ -692,20 +702,23 @@ def equal_error_study(pkg, torch, args):
     seeds in MIXED and FP64: posterior mean and std of every geometry
     parameter, evidence, stage counts and per-stage timing, written as JSON."""
     km, kf = (int(x) for x in args.study_seeds.split(","))
+    om, of = (int(x) for x in args.study_seed0.split(","))
     w, obs, rg, th_true, s_true = nested_workload(pkg, "c0")
     runs = {"mixed": [], "fp64": []}
-    for name, prec, k in (("mixed", pkg.PREC_MIXED, km), ("fp64", pkg.PREC_FP64, kf)):
-        for seed in range(1, k + 1):
+    for name, prec, k, off in (("mixed", pkg.PREC_MIXED, km, om), ("fp64", pkg.PREC_FP64, kf, of)):
+        for seed in range(off + 1, off + k + 1):
             t0 = time.perf_counter()
-            r = timed_outer_run(pkg, w, obs, rg, prec, 1000 + seed)
+            r = timed_outer_run(pkg, w, obs, rg, prec, seed)
             p = r["parts"]
-            runs[name].append({"seed": 1000 + seed, "evidence": r["evidence"], "nstage": r["nstage"],
+            runs[name].append({"seed": seed, "evidence": r["evidence"], "nstage": r["nstage"],
                                "wall_s": time.perf_counter() - t0, "mean": p.mean(0).tolist(),
                                "std": p.std(0).tolist(), "stage_s": [round(float(x), 4) for x in r["stage_s"]],
                                "stats": r["stats"]})
             print(name, seed, r["nstage"], r["evidence"], round(time.perf_counter() - t0, 1), flush=True)
     summ = {}
     for name in runs:
+        if not runs[name]:
+            continue
         m = np.array([x["mean"] for x in runs[name]])
         sd = np.array([x["std"] for x in runs[name]])
         ev = np.array([x["evidence"] for x in runs[name]])
@@ -713,22 +726,50 @@ def equal_error_study(pkg, torch, args):
                       "se_of_means": (m.std(0, ddof=1) / np.sqrt(len(m))).tolist() if len(m) > 1 else None,
                       "mean_of_stds": sd.mean(0).tolist(), "evidence_mean": float(ev.mean()),
                       "evidence_se": float(ev.std(ddof=1) / np.sqrt(len(ev))) if len(ev) > 1 else None}
-    mm, mf = np.array(summ["mixed"]["mean_of_means"]), np.array(summ["fp64"]["mean_of_means"])
-    sdm, sdf = np.array(summ["mixed"]["mean_of_stds"]), np.array(summ["fp64"]["mean_of_stds"])
     width = rg[:, 1] - rg[:, 0]
-    log("evidence and slip posterior, 512 streams per geometry")
-    ee = equal_error_c0(pkg, w, obs, rg, th_true, reps=512)
+    ee = None
+    if not args.study_no_evidence:
+        log("evidence and slip posterior, 512 streams per geometry")
+        ee = equal_error_c0(pkg, w, obs, rg, th_true, reps=512)
     res = {"workload": "c0 (8x4 patches, D = 64, 60 GNSS stations, 500 outer x 500 inner particles, ntau 50)",
            "evidence_and_slip": ee,
            "parameters": ["x", "y", "top", "length", "width", "strike", "dip", "log_alpha2"],
-           "true_theta": th_true.tolist(), "prior_range": rg.tolist(), "runs": runs, "summary": summ,
-           "posterior_mean_rel_diff": ((mm - mf) / np.abs(mf)).tolist(),
-           "posterior_mean_diff_rel_prior_width": ((mm - mf) / width).tolist(),
-           "posterior_std_rel_diff": ((sdm - sdf) / sdf).tolist(),
-           "evidence_diff": summ["mixed"]["evidence_mean"] - summ["fp64"]["evidence_mean"]}
+           "true_theta": th_true.tolist(), "prior_range": rg.tolist(), "runs": runs, "summary": summ}
+    if "mixed" in summ and "fp64" in summ:
+        mm, mf = np.array(summ["mixed"]["mean_of_means"]), np.array(summ["fp64"]["mean_of_means"])
+        sdm, sdf = np.array(summ["mixed"]["mean_of_stds"]), np.array(summ["fp64"]["mean_of_stds"])
+        res.update({"posterior_mean_rel_diff": ((mm - mf) / np.abs(mf)).tolist(),
+                    "posterior_mean_diff_rel_prior_width": ((mm - mf) / width).tolist(),
+                    "posterior_std_rel_diff": ((sdm - sdf) / sdf).tolist(),
+                    "evidence_diff": summ["mixed"]["evidence_mean"] - summ["fp64"]["evidence_mean"]})
     with open(args.equal_error_study, "w") as f:
         json.dump(res, f, indent=1)
-    print(json.dumps({k: res[k] for k in ("posterior_mean_rel_diff", "posterior_std_rel_diff", "evidence_diff")}))
+    print(json.dumps({k: res[k] for k in ("posterior_mean_rel_diff", "posterior_std_rel_diff", "evidence_diff")
+                      if k in res}))
+
+
+def equal_error_points(pkg, spec, reps=512):
+    """-log Z of the c0 nested evaluation in MIXED and FP64 at given
+    geometries, `reps` independent streams each: mean, spread, median,
+    minimum and the log of the mean evidence per precision."""
+    w, obs, rg, th_true, s_true = nested_workload(pkg, "c0")
+    ths = np.array([[float(v) for v in t.split(",")] for t in spec.split(";")])
+    thr = np.repeat(ths, reps, axis=0)
+    st = np.arange(len(thr), dtype=np.uint64)
+    res = {}
+    for name, prec in (("mixed", pkg.PREC_MIXED), ("fp64", pkg.PREC_FP64)):
+        g = pkg.SmcGpu(w.settings, prec)
+        g.set_data(obs)
+        v, s = g.fault_calc_likelihood(thr, 99, st + (0 if name == "fp64" else 10**6))
+        res[name] = v.reshape(len(ths), reps)
+        print(name, "status max", int(s.max()), flush=True)
+        g.close()
+    for i in range(len(ths)):
+        a, b = res["mixed"][i], res["fp64"][i]
+        se = np.sqrt((a.var(ddof=1) + b.var(ddof=1)) / reps)
+        print(f"theta {i}: mixed {a.mean():.4f} (sd {a.std():.3f}, med {np.median(a):.3f}, min {a.min():.3f}) "
+              f"fp64 {b.mean():.4f} (sd {b.std():.3f}, med {np.median(b):.3f}, min {b.min():.3f})  "
+              f"diff {a.mean() - b.mean():+.4f} se {se:.4f}")
 
 
 def main():
