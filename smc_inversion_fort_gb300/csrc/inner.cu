@@ -26,7 +26,8 @@ const char *inner_size_limit(int mixed, int engine, int D, int N) {
 
 long long inner_launch_key(int mixed, int engine, int D, int warps, int n_total) {
     // family: 1 GL32, 2 GL64, 3 FP64 CUDA cores, 4 MMA streamed, 5 MMA wide,
-    // 6 MMA pair, 7 tcgen05, 8 FP32 CUDA cores; row tile as the families pick it
+    // 6 MMA pair, 7 tcgen05, 8 FP32 CUDA cores, 9 MMA quad; row tile as the
+    // families pick it
     int fam, rt;
     if (inner_uses_global(mixed, engine, D)) {
         fam = mixed ? 1 : 2;
@@ -41,7 +42,7 @@ long long inner_launch_key(int mixed, int engine, int D, int warps, int n_total)
         int nsm = 0, dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        fam = n_total <= nsm ? 5 : 6;
+        fam = n_total <= nsm ? 5 : (D <= 64 && n_total > 2 * nsm) ? 9 : 6;
         rt = D <= 32 ? 2 : D <= 64 ? 4 : 8;
     } else if (engine == SMCGPU_ENGINE_TCGEN05 && D <= 128) {
         fam = 7;
@@ -102,11 +103,18 @@ cudaError_t launch_inner_parts(const InnerParts &P, cudaStream_t s, const char *
         return launch_inner_mma_streamed(P, s);
     } else if (a.engine == SMCGPU_ENGINE_MMA) {
         // 16 warps per geometry while the batch leaves SMs free (lowest
-        // latency per geometry), 8 warps and two geometries per CTA beyond
+        // latency per geometry), 8 warps and two geometries per CTA up to two
+        // geometries per SM; beyond, up to 64 slip dimensions, 4 warps and 16
+        // chain slots per geometry and four geometries per CTA (more geometries
+        // in flight per SM: the step chain is latency-bound, and the slots of a
+        // geometry are half idle anyway, the rounds of a stage being set by its
+        // longest Metropolis chain)
         int nsm = 0, dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        return ntot <= nsm ? launch_inner_mma_wide(P, s) : launch_inner_mma_pair(P, s);
+        if (ntot <= nsm) return launch_inner_mma_wide(P, s);
+        if (D <= 64 && ntot > 2 * nsm) return launch_inner_mma_quad(P, s);
+        return launch_inner_mma_pair(P, s);
     } else if (a.engine == SMCGPU_ENGINE_TCGEN05 && D <= 128) {
         return launch_inner_tc(P, s);
     }

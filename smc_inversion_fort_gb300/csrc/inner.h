@@ -82,6 +82,7 @@ cudaError_t launch_inner_cc32_wide(const InnerParts &P, cudaStream_t s, int W); 
 cudaError_t launch_inner_cc32_192(const InnerParts &P, cudaStream_t s, int W);       // 128 < D <= 192
 cudaError_t launch_inner_mma_wide(const InnerParts &P, cudaStream_t s);              // D <= 128
 cudaError_t launch_inner_mma_pair(const InnerParts &P, cudaStream_t s);              // D <= 128
+cudaError_t launch_inner_mma_quad(const InnerParts &P, cudaStream_t s);              // D <= 64
 cudaError_t launch_inner_mma_streamed(const InnerParts &P, cudaStream_t s);          // 128 < D <= 256
 cudaError_t launch_inner_tc(const InnerParts &P, cudaStream_t s);                    // D <= 128
 cudaError_t launch_inner_gl32(const InnerParts &P, cudaStream_t s);                  // D <= 1024

@@ -68,7 +68,11 @@ constexpr int CW = 8;    // chain slots per warp (CUDA-core engine)
 constexpr int CTW = 4;   // slots per lane
 constexpr int RGW = 16;  // row groups per warp
 constexpr uint32_t WAIT_TRIES = 1u << 22;   // bounded mbarrier wait
-enum : int { ENG_CC = 0, ENG_TC = 1, ENG_MMA = 2, ENG_GL = 3 };   // step engines
+// step engines; ENG_MMAQ is the warp-MMA engine with 16 chain slots per
+// geometry and the FP32 Gram matrix of the end-point energies read from global
+// memory (L2), so that four geometries of 4 warps share one SM (D <= 64)
+enum : int { ENG_CC = 0, ENG_TC = 1, ENG_MMA = 2, ENG_GL = 3, ENG_MMAQ = 4 };
+__host__ __device__ constexpr bool is_mma(int e) { return e == ENG_MMA || e == ENG_MMAQ; }
 
 // ---- warp-level tensor-core MMA (BF16 in, FP32 accumulate), m16n8k16
 __device__ __forceinline__ void ldsm_x4(uint32_t r[4], const void *p) {
@@ -482,7 +486,11 @@ struct Layout {
     // ring of the whole group takes GL_RING * DP * (GL_S / GL_SPT) entries
     static constexpr int GL_RING = (sizeof(T) == 8 && DP > 512) ? 6 : 16;
     static constexpr size_t GL_RING_BYTES = (size_t)GL_RING * DP * (GL_S / GL_SPT) * sizeof(T);
-    static constexpr int S = ENG == ENG_CC ? CW : ENG == ENG_GL ? GL_S : (AGL ? 4096 / DP : 2048 / DP);   // slots per warp (CC) / group
+    static constexpr int S = ENG == ENG_CC ? CW : ENG == ENG_GL ? GL_S : ENG == ENG_MMAQ ? 1024 / DP
+                             : (AGL ? 4096 / DP : 2048 / DP);   // slots per warp (CC) / group
+    // the FP32 Gram matrix of the end-point energies: in shared memory (warp
+    // MMA up to 128 dimensions) or read from global memory (AGL, MMAQ)
+    static constexpr bool A32_GLOBAL = AGL || ENG == ENG_MMAQ;
     static constexpr int RING = 6;                       // streamed k-tiles in flight per warp
     static constexpr uint32_t LBO_A = 2048;              // tcgen05: 128 rows x 16 B per k block
     static constexpr uint32_t LBO_B = 16 * S + 16;       // tcgen05: S rows x 16 B per k block, padded
@@ -501,9 +509,9 @@ struct Layout {
     __host__ __device__ static size_t engine_bytes(int W) {
         if (ENG == ENG_GL) return (size_t)DP * S * sizeof(T) + GL_RING_BYTES;  // step operand [row][slot], ring
         if (ENG == ENG_TC) return 2 * A_BYTES + 2 * B_BYTES;   // the end-point tile Xf aliases B
-        if (ENG == ENG_MMA)   // + the FP32 Gram matrix for the end-point energies (or the A ring)
+        if (is_mma(ENG))   // + the FP32 Gram matrix for the end-point energies (or the A ring)
             return 2 * A_BYTES + 4 * B_BYTES + 3 * TILE_BYTES +
-                   (AGL ? ring_bytes(W) : (size_t)DP * DP * sizeof(float));
+                   (AGL ? ring_bytes(W) : A32_GLOBAL ? 0 : (size_t)DP * DP * sizeof(float));
         return (size_t)DP * DP * sizeof(T) + (size_t)W * 2 * DP * CW * sizeof(T);
     }
     __host__ __device__ static int slots(int W) { return ENG == ENG_CC ? W * CW : S; }
@@ -513,7 +521,7 @@ struct Layout {
         if (ENG == ENG_GL)   // per-warp, per-slot partial sums of 5 quantities (also 32 W floats of moments)
             return (size_t)5 * W * S * sizeof(double) > (size_t)32 * W * sizeof(float)
                        ? (size_t)5 * W * S * sizeof(double) : (size_t)32 * W * sizeof(float);
-        return ENG == ENG_MMA ? (size_t)5 * 32 * W * sizeof(float) : (size_t)5 * 32 * (W > 4 ? W : 4) * sizeof(double);
+        return is_mma(ENG) ? (size_t)5 * 32 * W * sizeof(float) : (size_t)5 * 32 * (W > 4 ? W : 4) * sizeof(double);
     }
     __host__ __device__ static size_t bytes(int W) {
         size_t b = engine_bytes(W) + (size_t)7 * DP * sizeof(T) + (size_t)6 * DP * sizeof(double) +
@@ -544,14 +552,14 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
     unsigned char *Ahi = nullptr, *Alo = nullptr, *Bhi = nullptr, *Blo = nullptr;
     float *Xf = nullptr, *tX = nullptr, *tP = nullptr, *tXC = nullptr, *tA32 = nullptr;
     uint4 *aring = nullptr;
-    if constexpr (ENG == ENG_MMA) {
+    if constexpr (is_mma(ENG)) {
         // B buffer b: hi at Bhi + 2*b*B_BYTES, lo B_BYTES after it
         Ahi = sp; Alo = Ahi + L_::A_BYTES; Bhi = Alo + L_::A_BYTES; Blo = Bhi + L_::B_BYTES;
         tX = (float *)(Bhi + 4 * L_::B_BYTES);
         tP = (float *)((unsigned char *)tX + L_::TILE_BYTES);
         tXC = (float *)((unsigned char *)tP + L_::TILE_BYTES);
         if constexpr (L_::AGL) aring = (uint4 *)((unsigned char *)tXC + L_::TILE_BYTES);
-        else tA32 = (float *)((unsigned char *)tXC + L_::TILE_BYTES);
+        else if constexpr (!L_::A32_GLOBAL) tA32 = (float *)((unsigned char *)tXC + L_::TILE_BYTES);
         static_assert(2 * L_::B_BYTES >= L_::TILE_BYTES, "offset tile must fit in one B buffer");
     } else if constexpr (ENG == ENG_GL) {
         Msm = nullptr;
@@ -615,8 +623,8 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
     float *lv32 = a.lv32 ? a.lv32 + (size_t)th * m.nrow * 9 : nullptr;
     float *ll32 = a.ll32 ? a.ll32 + (size_t)th * m.ll_nnz : nullptr;
     float *wf = (float *)(Lc + 8 * N);   // MIXED: FP32 copy of the normalised weights
-    if constexpr (ENG == ENG_MMA) {
-        if constexpr (L_::AGL) {
+    if constexpr (is_mma(ENG)) {
+        if constexpr (L_::A32_GLOBAL) {
             for (int e = gt; e < D * D; e += gnt) A32[e] = (float)Ath[e];
         } else {
             for (int e = gt; e < DP * DP; e += gnt) {
@@ -876,9 +884,10 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                 fr[(size_t)(2 * tile) * 32 + ln] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
                 fr[(size_t)(2 * tile + 1) * 32 + ln] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
             }
-        } else if constexpr (ENG == ENG_MMA) {
+        } else if constexpr (is_mma(ENG)) {
             // M = gamma A + L^T L / alpha^2 in FP32 (A from the FP32 copy in shared
-            // memory), split into BF16 hi + lo, row-major with row stride DP+8;
+            // memory, or in global memory for MMAQ), split into BF16 hi + lo,
+            // row-major with row stride DP+8;
             // TPR threads per row, KC consecutive columns each
             const float gf = (float)gamma, ia2 = (float)(1.0 / alpha2);
             const int TPR = gnt / DP, KC = DP / TPR;
@@ -892,7 +901,8 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                 for (int k = k0; k < k0 + KC; ++k) {
                     float v = 0.0f;
                     if (i < D && k < D) {
-                        v = gf * tA32[k * DP + i];
+                        if constexpr (L_::A32_GLOBAL) v = gf * A32[(size_t)k * D + i];
+                        else v = gf * tA32[k * DP + i];
                         if (e < e1 && m.ll_col[e] == k) { v += ll32[e] * ia2; ++e; }
                     }
                     tc::split_bf16(v, rh[k], rl[k]);
@@ -1030,7 +1040,7 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                     }
                 }
             }
-            if constexpr (ENG == ENG_MMA) {
+            if constexpr (is_mma(ENG)) {
                 // ================= warp-MMA engine: S slots per group.
                 // Step layout: warp wl owns m-tiles mt0.. (16 dimensions each) x
                 // n-tiles nt0.. (8 slots each); lane (g, t4) holds rows 16 mt + g and
@@ -1367,11 +1377,28 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                                 }
                         }
                     } else if (slot_on) {
-                        for (int k = 0; k < D; ++k) {
-                            const float dk = dl[k * TS + cs];
-                            const float *ak = tA32 + k * DP + part;
+                        if constexpr (L_::A32_GLOBAL) {
+                            // MMAQ: the FP32 Gram matrix from global memory (column-major,
+                            // leading dimension D; L1/L2-resident), rows >= D skipped
+                            const float *Ag = A32 + part;
+                            bool rl[RPT];
 #pragma unroll
-                            for (int i = 0; i < RPT; ++i) af[i] = fmaf(ak[i * NPART], dk, af[i]);
+                            for (int i = 0; i < RPT; ++i) rl[i] = part + i * NPART < D;
+#pragma unroll 4
+                            for (int k = 0; k < D; ++k) {
+                                const float dk = dl[k * TS + cs];
+                                const float *ak = Ag + (size_t)k * D;
+#pragma unroll
+                                for (int i = 0; i < RPT; ++i)
+                                    if (rl[i]) af[i] = fmaf(ak[i * NPART], dk, af[i]);
+                            }
+                        } else {
+                            for (int k = 0; k < D; ++k) {
+                                const float dk = dl[k * TS + cs];
+                                const float *ak = tA32 + k * DP + part;
+#pragma unroll
+                                for (int i = 0; i < RPT; ++i) af[i] = fmaf(ak[i * NPART], dk, af[i]);
+                            }
                         }
                     }
                     if (slot_on) {
@@ -2364,7 +2391,7 @@ __device__ __forceinline__ void inner_group_entry(const InnerParts &P, int W, in
 }
 
 template <typename T, int RT, int ENG, int WG>
-__global__ void __launch_bounds__(ENG == ENG_MMA ? 512 : 256) inner_group_kernel(const __grid_constant__ InnerParts P,
+__global__ void __launch_bounds__(is_mma(ENG) ? 512 : 256) inner_group_kernel(const __grid_constant__ InnerParts P,
                                                                                int W, int G) {
     inner_group_entry<T, RT, ENG, WG>(P, W, G);
 }

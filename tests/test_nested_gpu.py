@@ -245,6 +245,32 @@ def test_nested_mixed_latency_configuration_matches_fp64(smcgpu, orc):
     assert abs(np.median(a) - np.median(b)) < 4 * 1.2533 * se + 1e-9
 
 
+@pytest.mark.parametrize("name", ["tiny", "c0"])
+def test_nested_mixed_quad_configuration_matches_fp64(smcgpu, orc, name):
+    """Batches of more than two geometries per SM at up to 64 slip dimensions
+    run the MIXED warp-MMA engine with 4 warps and 16 chain slots per
+    geometry, four geometries per CTA (the Gram matrix of the end-point
+    energies read from global memory).  One batch of 2 x SM count + 16
+    evaluations at the true geometry against FP64: mean and median -log Z
+    within 4 standard errors."""
+    import torch
+    w, obs, o = setup_case(name, orc)
+    th = true_theta(w)
+    n = 2 * torch.cuda.get_device_properties(0).multi_processor_count + 16
+    g64 = smcgpu.SmcGpu(w.settings, smcgpu.PREC_FP64)
+    g64.set_data(obs)
+    g32 = smcgpu.SmcGpu(w.settings, smcgpu.PREC_MIXED)
+    g32.set_data(obs)
+    st = np.arange(n, dtype=np.uint64) + 12000
+    a, sa = g64.fault_calc_likelihood(np.repeat(th[None], n, 0), 29, st)
+    b, sb = g32.fault_calc_likelihood(np.repeat(th[None], n, 0), 29, st + 10**6)
+    assert np.all(sa == 0) and np.all(sb == 0)
+    se = np.sqrt((a.var(ddof=1) + b.var(ddof=1)) / n)
+    print("fp64", a.mean(), np.median(a), "mixed", b.mean(), np.median(b), "se", se)
+    assert abs(a.mean() - b.mean()) < 4 * se + 1e-9
+    assert abs(np.median(a) - np.median(b)) < 4 * 1.2533 * se + 1e-9
+
+
 def test_posterior_population(smcgpu, orc):
     """Final inner population (the reference's slip output) against the
     oracle: per stream the two agree to rounding until a rounding-level
