@@ -1118,8 +1118,9 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
 #pragma unroll
                             for (int h = 0; h < 2; ++h) {
                                 const int r = 16 * (mt0 + aa) + g + 8 * h, c0 = 8 * (nt0 + bb) + 2 * t4;
-                                const float d0 = live_l[aa][h] ? x[aa][bb][2 * h] - mean_l[aa][h] : 0.0f;
-                                const float d1 = live_l[aa][h] ? x[aa][bb][2 * h + 1] - mean_l[aa][h] : 0.0f;
+                                // rows beyond D hold x = 0 and mean 0: their offsets are 0
+                                const float d0 = x[aa][bb][2 * h] - mean_l[aa][h];
+                                const float d1 = x[aa][bb][2 * h + 1] - mean_l[aa][h];
                                 const __nv_bfloat162 hi = __floats2bfloat162_rn(d0, d1);
                                 const __nv_bfloat162 lo = __floats2bfloat162_rn(d0 - __low2float(hi), d1 - __high2float(hi));
                                 *(uint32_t *)(bh + r * BST + c0) = bf16x2_bits(hi);
@@ -1193,7 +1194,11 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                         dts[bb][0] = (float)sdt[c0];
                         dts[bb][1] = (float)sdt[c0 + 1];
                     }
-                    bool on[MTW][NTW][4];
+                    // Entries of idle slots and of rows beyond D start at x = p = 0 and
+                    // idle slots have step size 0 (sdt), so the step below leaves them
+                    // unchanged without a per-entry select: the rows beyond D have zero
+                    // gradient (M, c and the stage mean are 0 there), and an idle slot's
+                    // momentum and position updates are multiplied by its zero step size.
                     float cdt[MTW][NTW][4];
 #pragma unroll
                     for (int aa = 0; aa < MTW; ++aa)
@@ -1201,23 +1206,16 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                         for (int bb = 0; bb < NTW; ++bb)
 #pragma unroll
                             for (int e = 0; e < 4; ++e) {
-                                const int c = 8 * (nt0 + bb) + 2 * t4 + (e & 1);
-                                on[aa][bb][e] = live_l[aa][e >> 1] && ((actm >> c) & 1ull);
-                                cdt[aa][bb][e] = cov_l[aa][e >> 1] * dts[bb][e & 1];
-                            }
-#pragma unroll
-                    for (int aa = 0; aa < MTW; ++aa)
-#pragma unroll
-                        for (int bb = 0; bb < NTW; ++bb)
-#pragma unroll
-                            for (int e = 0; e < 4; ++e) {
                                 const int r = 16 * (mt0 + aa) + g + 8 * (e >> 1), c = 8 * (nt0 + bb) + 2 * t4 + (e & 1);
-                                x[aa][bb][e] = tXC[r * TS + c];
-                                p[aa][bb][e] = tP[r * TS + c];
+                                const bool on = live_l[aa][e >> 1] && ((actm >> c) & 1ull);
+                                cdt[aa][bb][e] = cov_l[aa][e >> 1] * dts[bb][e & 1];
+                                x[aa][bb][e] = on ? tXC[r * TS + c] : 0.0f;
+                                p[aa][bb][e] = on ? tP[r * TS + c] : 0.0f;
                             }
                     write_b(0);
                     // leapfrog (smc_slip.f90:755-904): P/2 (X P)^ntau X/2
                     int flag = 0;
+                    unsigned frozen = 0u;   // this thread's entries of chains that blew up
                     for (int it = 0; it <= a.ntau; ++it) {
                         grp.sync();
                         const unsigned long long blm = masks[2];
@@ -1284,7 +1282,23 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                                 for (int e = 0; e < 4; ++e) acc[aa][bb][e] += acc1[aa][bb][e] + acc2[aa][bb][e];
                         // momentum and position updates with the step factors of this
                         // step; the reflection / blow-up path only for entries that left
-                        // [0, max_slip]; chains that blew up stay frozen
+                        // [0, max_slip]; chains that blew up stay frozen: their step
+                        // size becomes 0 from the step after (rare, warp-uniform branch)
+                        if (blm != 0ull) {
+#pragma unroll
+                            for (int bb = 0; bb < NTW; ++bb)
+#pragma unroll
+                                for (int j = 0; j < 2; ++j)
+                                    if ((blm >> (8 * (nt0 + bb) + 2 * t4 + j)) & 1ull) {
+                                        dts[bb][j] = 0.0f;
+#pragma unroll
+                                        for (int aa = 0; aa < MTW; ++aa) {
+                                            cdt[aa][bb][j] = 0.0f;
+                                            cdt[aa][bb][2 + j] = 0.0f;
+                                            frozen |= (1u << ((aa * NTW + bb) * 4 + j)) | (1u << ((aa * NTW + bb) * 4 + 2 + j));
+                                        }
+                                    }
+                        }
                         const float hs = it == 0 ? 0.5f : 1.0f, xs = it == a.ntau ? 0.5f : 1.0f;
                         // common step: update and one range test; entries that left the
                         // box (reflection, or |x| > 1e3: the chain blows up) go through a
@@ -1296,17 +1310,16 @@ __device__ __forceinline__ void group_body(const MeshDev &m, const InnerArgs &a,
                             for (int bb = 0; bb < NTW; ++bb)
 #pragma unroll
                                 for (int e = 0; e < 4; ++e) {
-                                    const int h = e >> 1, c = 8 * (nt0 + bb) + 2 * t4 + (e & 1);
-                                    bool live = on[aa][bb][e];
-                                    if (blm != 0ull) live = live && !((blm >> c) & 1ull);
+                                    const int h = e >> 1;
                                     const float gr = cv_l[aa][h] + acc[aa][bb][e];
                                     const float pn = p[aa][bb][e] - gr * (hs * dts[bb][e & 1]);
                                     const float xn = x[aa][bb][e] + cdt[aa][bb][e] * xs * pn;
-                                    x[aa][bb][e] = live ? xn : x[aa][bb][e];
-                                    p[aa][bb][e] = live ? pn : p[aa][bb][e];
+                                    x[aa][bb][e] = xn;
+                                    p[aa][bb][e] = pn;
                                     const bool out = !(xn >= 0.0f && xn <= mx);
-                                    outmask |= (live && out) ? 1u << ((aa * NTW + bb) * 4 + e) : 0u;
+                                    outmask |= out ? 1u << ((aa * NTW + bb) * 4 + e) : 0u;
                                 }
+                        outmask &= ~frozen;   // a blown chain keeps its last state
                         if (__any_sync(FULL, outmask != 0u)) {
 #pragma unroll
                             for (int aa = 0; aa < MTW; ++aa)
