@@ -1393,6 +1393,40 @@ extern "C" int orc_fault_likelihood(const orc_setup *s, const double *theta, uin
     return in.status;
 }
 
+// The inner target's pieces at one slip vector x for geometry theta: the
+// likelihood (slip_calc_likelihood, smc_slip.f90:56-104), the prior
+// (slip_calc_prior, :106-137) and the tempered gradient gamma * dL/dx + dP/dx
+// (slip_calc_grad, :139-182), on the same G, Gram products and Laplacian as
+// orc_fault_likelihood.  For the finite-difference check of the gradient.
+extern "C" int orc_slip_energy(const orc_setup *s, const double *theta, double gamma, const double *x,
+                               double *lik, double *pri, double *grad) {
+    std::vector<Plane> pl;
+    planes_of(s, theta, pl);
+    Mesh m;
+    discretize(s, pl, m);
+    Lap lp;
+    laplacian_impl(s, pl, m, lp);
+    int D = m.D, nobs = s->nobs;
+    std::vector<double> gmat((size_t)nobs * D);
+    greens_impl(s, pl, m, gmat.data());
+    double la2, lsar, lgnss;
+    orc_hyper(s, theta, &la2, &lsar, &lgnss);
+    std::vector<double> A((size_t)D * D), b(D);
+    double dsd;
+    orc_gram(s, gmat.data(), exp(lsar), exp(lgnss), A.data(), b.data(), &dsd);
+    Inner in;
+    in.D = D; in.N = 1; in.nrow = lp.nrow;
+    in.A = A.data(); in.b = b.data(); in.dsd = dsd; in.LL = lp.ll.data();
+    in.lidx = lp.lidx.data(); in.lval = lp.lval.data(); in.ltidx = lp.ltidx.data(); in.ltval = lp.ltval.data();
+    in.alpha2.assign(lp.nrow, exp(la2));
+    in.lsar = lsar; in.lgnss = lgnss; in.nsar_total = s->nsar_total; in.ngnss = s->ngnss;
+    std::vector<double> ls(lp.nrow);
+    *lik = likelihood(in, x);
+    *pri = prior(in, x);
+    gradient(in, x, gamma, grad, ls.data());
+    return D;
+}
+
 extern "C" int orc_fault_likelihood_batch(const orc_setup *s, int32_t n, const double *theta, uint64_t seed,
                                           const uint64_t *streams, double *neglog, int32_t *status,
                                           int32_t nthreads) {

@@ -98,6 +98,9 @@ int orc_fault_likelihood(const orc_setup *s, const double *theta, uint64_t seed,
                          double *neglog, double *particles /* optional N x D */,
                          double *likelihood /* optional N */, double *prior /* optional N */,
                          orc_inner_trace *trace /* optional */);
+// likelihood, prior and tempered gradient gamma dL/dx + dP/dx at one slip vector (returns D)
+int orc_slip_energy(const orc_setup *s, const double *theta, double gamma, const double *x, double *lik, double *pri,
+                    double *grad);
 int orc_fault_likelihood_batch(const orc_setup *s, int32_t n, const double *theta, uint64_t seed,
                                const uint64_t *streams, double *neglog, int32_t *status, int32_t nthreads);
 int orc_greens_batch(const orc_setup *s, int32_t n, const double *theta, double *gmat, int32_t nthreads);

@@ -90,6 +90,8 @@ def lib() -> C.CDLL:
         L.orc_fault_likelihood.argtypes = [vp, vp, u64, u64, vp, vp, vp, vp, vp]
         L.orc_fault_likelihood.restype = i32
         L.orc_fault_likelihood_batch.argtypes = [vp, i32, vp, u64, vp, vp, vp, i32]
+        L.orc_slip_energy.argtypes = [vp, vp, d, vp, vp, vp, vp]
+        L.orc_slip_energy.restype = i32
         L.orc_resample.argtypes = [vp, i32, d, d, vp]
         L.orc_qsort_.argtypes = [vp, vp, vp]
         L.orc_fault_smc.argtypes = [vp, vp, i32, i32, u64, i32, vp, vp, vp, vp, vp, vp]
@@ -209,6 +211,15 @@ class Oracle:
             n = tr.nstage
             out.update(gamma=gam[:n].copy(), neglog_inc=inc[:n].copy(), assigned=asg[:n].copy())
         return out
+
+    def slip_energy(self, theta, gamma, x):
+        """Likelihood, prior and the tempered gradient gamma dL/dx + dP/dx at slip x."""
+        th = np.ascontiguousarray(theta, np.float64)
+        xv = np.ascontiguousarray(x, np.float64)
+        grad = np.zeros(self.dims["D"])
+        lik, pri = C.c_double(), C.c_double()
+        lib().orc_slip_energy(C.byref(self.st), _p(th), float(gamma), _p(xv), C.byref(lik), C.byref(pri), _p(grad))
+        return lik.value, pri.value, grad
 
     def fault_likelihood_batch(self, thetas, seed, streams, nthreads=0):
         th = np.ascontiguousarray(thetas, np.float64)

@@ -143,3 +143,42 @@ def test_laplacian_operator(orc):
             for q in range(9):
                 Lt[lti[c, q], c] += ltv[c, q]
         np.testing.assert_array_equal(L, Lt)
+
+
+@pytest.mark.parametrize("name", ["tiny-nodal", "c0", "tiny-2plane"])
+def test_slip_gradient_matches_finite_differences(orc, name):
+    """The leapfrog's force, slip_calc_grad (smc_slip.f90:139-182), against
+    central finite differences of the tempered target gamma L(x) + P(x)
+    (slip_calc_likelihood :56-104, slip_calc_prior :106-137) on the same
+    Green's matrix, Gram products and Laplacian, at random slip vectors:
+    the check the reference kept as a commented hook (smc_slip.f90:829-845)."""
+    from smc_inversion_fort_gb300.configs import make_stations, preset, random_thetas, true_slip, true_theta
+    w = preset(name)
+    rng = np.random.default_rng(5)
+    obs = make_stations(w, rng)
+    o0 = orc.Oracle(w.settings, obs)
+    d = o0.greens(true_theta(w)).T @ true_slip(w)
+    obs["dvec"] = d + rng.standard_normal(len(d)) * obs["obs_sigma"]
+    o = orc.Oracle(w.settings, obs)
+    ths = np.vstack([true_theta(w)[None], random_thetas(w, 1, seed=8)])
+    D = o.dims["D"]
+    for th in ths:
+        for gamma in (0.3, 1.0):
+            x = rng.uniform(0.1, 1.5, D)
+            lik, pri, grad = o.slip_energy(th, gamma, x)
+            assert np.isfinite(lik) and np.isfinite(pri)
+            fd = np.zeros(D)
+            for i in range(D):
+                h = 1e-4 * max(1.0, abs(x[i]))
+                xp, xm = x.copy(), x.copy()
+                xp[i] += h
+                xm[i] -= h
+                lp, pp, _ = o.slip_energy(th, gamma, xp)
+                lm, pm, _ = o.slip_energy(th, gamma, xm)
+                fd[i] = ((gamma * lp + pp) - (gamma * lm + pm)) / (2 * h)
+            scale = np.abs(grad).max()
+            # the target is quadratic in x: central differences are exact up
+            # to the rounding of the energies (about 1e-16 |energy| / h)
+            tol = 1e-8 * scale + 1e-14 * (abs(gamma * lik) + abs(pri)) / 1e-4
+            print(name, gamma, "max |fd - grad|", np.abs(fd - grad).max(), "scale", scale, "tol", tol)
+            assert np.abs(fd - grad).max() <= tol
