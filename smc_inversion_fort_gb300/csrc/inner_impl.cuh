@@ -2417,12 +2417,19 @@ __global__ void __launch_bounds__(512, 1) inner_gl_kernel(const __grid_constant_
 }
 
 // CTAs of a persistent launch: one wave (resident CTAs), no more than the
-// geometries need; the queue counter is reset on the launch's stream.
-// Without a queue, one CTA per G geometries.
+// geometries need, but one CTA per SM as long as there are at least as many
+// geometries as SMs (a batch of 500 geometries in CTAs of four groups then
+// spreads over all 152 SMs instead of filling 125); the queue counter is
+// reset on the launch's stream.  Without a queue, one CTA per G geometries.
 static unsigned persistent_blocks(const InnerParts &P, int G, int resident, cudaStream_t s) {
-    const int need = (P.start[P.n] + G - 1) / G;
+    const int ntot = P.start[P.n];
+    int need = (ntot + G - 1) / G;
     int *queue = P.a[0].queue;
     if (!queue) return (unsigned)need;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    need = std::max(need, std::min(ntot, nsm));
     if (cudaMemsetAsync(queue, 0, sizeof(int), s) != cudaSuccess) return 0;
     return (unsigned)std::max(1, std::min(need, resident));
 }
