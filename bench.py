@@ -370,7 +370,10 @@ def nested_c2_bench(pkg, torch, cpu=True, fp64_sample=152, sample_stages=2):
            "mixed": {"outer_particles_per_s": w.n_outer / float(ss[0]), "s_outer_stage": float(ss[0]),
                      "stage_evals": int(r["stage_evals"][0]),
                      "nested_evals_per_s": float(r["stage_evals"][0] / ss[0]), "init_eval_s": r["init_s"],
-                     "mean_inner_stages": st["inner_stages"] / max(st["nested_evals"], 1)}}
+                     "mean_inner_stages": st["inner_stages"] / max(st["nested_evals"], 1),
+                     "roofline_inner": inner_roofline(st, w.settings.ntau, w.settings.dims()["D"],
+                                                      PEAKS.get("bf16_tflops_sustained", 1700.0),
+                                                      "bf16_tflops_sustained (MEASURED_PEAKS.json)")}}
     # FP64 against MIXED on one wave of prior geometries
     from smc_inversion_fort_gb300.configs import random_thetas
     th = random_thetas(w, fp64_sample, seed=12)
