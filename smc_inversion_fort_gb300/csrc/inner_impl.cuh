@@ -235,10 +235,12 @@ __device__ __forceinline__ double wreduce_n(double v[NV], int lane) {
     return t;
 }
 
-// 4- or 8-byte asynchronous global -> shared copy (through L1), in commit groups
+// 4- or 8-byte asynchronous global -> shared copy (through L1), in commit
+// groups; src_bytes = 0 writes zeros and reads nothing
 template <int BYTES>
-__device__ __forceinline__ void cp_async_small(void *dst, const void *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(tc::smem_u32(dst)), "l"(src), "n"(BYTES)
+__device__ __forceinline__ void cp_async_zfill(void *dst, const void *src, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(tc::smem_u32(dst)), "l"(src), "n"(BYTES),
+                 "r"(src_bytes)
                  : "memory");
 }
 // (d0, d1) += a * (b0, b1) as one packed FP32x2 FMA: each lane is an FP32 fma,
@@ -267,57 +269,74 @@ __device__ __forceinline__ void ffma2(float &d0, float &d1, float a, float b0, f
 template <typename T, int R, int SPT, int RP, int S, int P, int NTH>
 __device__ __forceinline__ void gl_gemm(const T *Mg, int D, const T *__restrict__ X, int row0, int s0,
                                         T *ring, int tid, T acc[R][SPT]) {
+    static_assert(P % 2 == 0, "columns are streamed in pairs");
 #pragma unroll
     for (int i = 0; i < R; ++i)
 #pragma unroll
         for (int q = 0; q < SPT; ++q) acc[i][q] = T(0);
-    bool live[R];
+    // the thread's rows; rows beyond D (and columns beyond D) are copied as
+    // zeros (cp.async zero fill, nothing read) from a clamped in-bounds address,
+    // so the product loop needs no per-entry select
+    int rowc[R], bytes_r[R];
 #pragma unroll
-    for (int i = 0; i < R; ++i) live[i] = row0 + i * RP < D;
+    for (int i = 0; i < R; ++i) {
+        const bool live = row0 + i * RP < D;
+        rowc[i] = live ? row0 + i * RP : D - 1;
+        bytes_r[i] = live ? (int)sizeof(T) : 0;
+    }
     T *my = ring + tid;
-    auto issue = [&](int k, int slot) {
-        if (k < D) {
-            const T *src = Mg + (size_t)k * D + row0;
+    // columns k and k + 1 into ring slots slot and slot + 1, one commit group per pair
+    auto issue_pair = [&](int k, int slot) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int kk = k + j;
+            const bool col = kk < D;
+            const T *src = Mg + (size_t)(col ? kk : D - 1) * D;
 #pragma unroll
             for (int i = 0; i < R; ++i)
-                if (live[i]) cp_async_small<sizeof(T)>(my + (slot * R + i) * NTH, src + i * RP);
+                cp_async_zfill<sizeof(T)>(my + ((slot + j) * R + i) * NTH, src + rowc[i], col ? bytes_r[i] : 0);
         }
-        cp_async_commit();   // empty groups past the last column keep the count uniform
+        cp_async_commit();
     };
 #pragma unroll
-    for (int kk = 0; kk < P; ++kk) issue(kk, kk);
+    for (int kk = 0; kk < P; kk += 2) issue_pair(kk, kk);
     int slot = 0;
-#pragma unroll 2
-    for (int k = 0; k < D; ++k) {
-        // groups committed: columns 0 .. k + P - 1; at most P - 1 pending means column k has landed
-        cp_async_wait<P - 1>();
-        T mv[R];
+    for (int k = 0; k < D; k += 2) {
+        // groups committed: column pairs 0 .. (k + P) / 2 - 1; at most P / 2 - 1
+        // pending means the pair (k, k + 1) has landed
+        cp_async_wait<P / 2 - 1>();
 #pragma unroll
-        for (int i = 0; i < R; ++i) mv[i] = live[i] ? my[(slot * R + i) * NTH] : T(0);
-        const T *xk = X + k * S + s0;   // 16-byte aligned: S and s0 are multiples of 8
-        if constexpr (sizeof(T) == 4) {
+        for (int j = 0; j < 2; ++j) {
+            T mv[R];
 #pragma unroll
-            for (int q = 0; q < SPT; q += 4) {
-                const float4 v = *reinterpret_cast<const float4 *>(xk + q);
+            for (int i = 0; i < R; ++i) mv[i] = my[((slot + j) * R + i) * NTH];
+            // column D (odd D only) is a zero-filled slot: its products add 0;
+            // the operand row D exists (X has DP >= D + 1 rows) and is zero
+            const T *xk = X + (k + j) * S + s0;   // 16-byte aligned: S and s0 are multiples of 8
+            if constexpr (sizeof(T) == 4) {
 #pragma unroll
-                for (int i = 0; i < R; ++i) {
-                    ffma2(acc[i][q], acc[i][q + 1], (float)mv[i], v.x, v.y);
-                    ffma2(acc[i][q + 2], acc[i][q + 3], (float)mv[i], v.z, v.w);
+                for (int q = 0; q < SPT; q += 4) {
+                    const float4 v = *reinterpret_cast<const float4 *>(xk + q);
+#pragma unroll
+                    for (int i = 0; i < R; ++i) {
+                        ffma2(acc[i][q], acc[i][q + 1], (float)mv[i], v.x, v.y);
+                        ffma2(acc[i][q + 2], acc[i][q + 3], (float)mv[i], v.z, v.w);
+                    }
                 }
-            }
-        } else {
+            } else {
 #pragma unroll
-            for (int q = 0; q < SPT; q += 2) {
-                const double2 v = *reinterpret_cast<const double2 *>(xk + q);
+                for (int q = 0; q < SPT; q += 2) {
+                    const double2 v = *reinterpret_cast<const double2 *>(xk + q);
 #pragma unroll
-                for (int i = 0; i < R; ++i) {
-                    acc[i][q] = fma((double)mv[i], v.x, (double)acc[i][q]);
-                    acc[i][q + 1] = fma((double)mv[i], v.y, (double)acc[i][q + 1]);
+                    for (int i = 0; i < R; ++i) {
+                        acc[i][q] = fma((double)mv[i], v.x, (double)acc[i][q]);
+                        acc[i][q + 1] = fma((double)mv[i], v.y, (double)acc[i][q + 1]);
+                    }
                 }
             }
         }
-        issue(k + P, slot);   // column k + P into the slot just consumed
-        slot = slot + 1 == P ? 0 : slot + 1;
+        issue_pair(k + P, slot);   // the next pair into the slots just consumed
+        slot = slot + 2 == P ? 0 : slot + 2;
     }
 }
 
