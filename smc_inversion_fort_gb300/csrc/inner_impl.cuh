@@ -269,7 +269,10 @@ __device__ __forceinline__ void ffma2(float &d0, float &d1, float a, float b0, f
 template <typename T, int R, int SPT, int RP, int S, int P, int NTH>
 __device__ __forceinline__ void gl_gemm(const T *Mg, int D, const T *__restrict__ X, int row0, int s0,
                                         T *ring, int tid, T acc[R][SPT]) {
-    static_assert(P % 2 == 0, "columns are streamed in pairs");
+    // columns travel in groups of CG (four when the ring holds a multiple of
+    // four columns, else pairs): one commit group and one wait per group
+    constexpr int CG = P % 4 == 0 ? 4 : 2;
+    static_assert(P % CG == 0, "the ring holds whole column groups");
 #pragma unroll
     for (int i = 0; i < R; ++i)
 #pragma unroll
@@ -285,10 +288,10 @@ __device__ __forceinline__ void gl_gemm(const T *Mg, int D, const T *__restrict_
         bytes_r[i] = live ? (int)sizeof(T) : 0;
     }
     T *my = ring + tid;
-    // columns k and k + 1 into ring slots slot and slot + 1, one commit group per pair
-    auto issue_pair = [&](int k, int slot) {
+    // columns k .. k + CG - 1 into ring slots slot .. slot + CG - 1, one commit group
+    auto issue_group = [&](int k, int slot) {
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
+        for (int j = 0; j < CG; ++j) {
             const int kk = k + j;
             const bool col = kk < D;
             const T *src = Mg + (size_t)(col ? kk : D - 1) * D;
@@ -299,19 +302,19 @@ __device__ __forceinline__ void gl_gemm(const T *Mg, int D, const T *__restrict_
         cp_async_commit();
     };
 #pragma unroll
-    for (int kk = 0; kk < P; kk += 2) issue_pair(kk, kk);
+    for (int kk = 0; kk < P; kk += CG) issue_group(kk, kk);
     int slot = 0;
-    for (int k = 0; k < D; k += 2) {
-        // groups committed: column pairs 0 .. (k + P) / 2 - 1; at most P / 2 - 1
-        // pending means the pair (k, k + 1) has landed
-        cp_async_wait<P / 2 - 1>();
+    for (int k = 0; k < D; k += CG) {
+        // groups committed: column groups 0 .. (k + P) / CG - 1; at most P / CG - 1
+        // pending means the group of columns k .. k + CG - 1 has landed
+        cp_async_wait<P / CG - 1>();
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
+        for (int j = 0; j < CG; ++j) {
             T mv[R];
 #pragma unroll
             for (int i = 0; i < R; ++i) mv[i] = my[((slot + j) * R + i) * NTH];
-            // column D (odd D only) is a zero-filled slot: its products add 0;
-            // the operand row D exists (X has DP >= D + 1 rows) and is zero
+            // columns past D are zero-filled slots: their products add 0; the
+            // operand rows past D exist (X has DP rows, a multiple of 256) and are zero
             const T *xk = X + (k + j) * S + s0;   // 16-byte aligned: S and s0 are multiples of 8
             if constexpr (sizeof(T) == 4) {
 #pragma unroll
@@ -335,8 +338,8 @@ __device__ __forceinline__ void gl_gemm(const T *Mg, int D, const T *__restrict_
                 }
             }
         }
-        issue_pair(k + P, slot);   // the next pair into the slots just consumed
-        slot = slot + 2 == P ? 0 : slot + 2;
+        issue_group(k + P, slot);   // the next group into the slots just consumed
+        slot = slot + CG == P ? 0 : slot + CG;
     }
 }
 
