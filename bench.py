@@ -74,6 +74,18 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(x, world, device):
+    """The job's time of a per-rank time: the maximum over the ranks (one
+    all_reduce MAX on the job's process group); x itself on one rank."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def workload(n_theta):
     from smc_inversion_fort_gb300.configs import make_stations, preset, random_thetas
     w = preset("c1")
@@ -601,11 +613,7 @@ def gb300_arm(args):
     if world > 1:
         tdist.barrier()
     clocks = clk.stop()
-    total_ms = t_start.elapsed_time(t_end)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(t_start.elapsed_time(t_end), world, dev)
     ms = total_ms / args.steps
     kern_ms = statistics.mean(a.elapsed_time(e) for a, e in evs)
     value = entries * world / (ms * 1e-3)
@@ -651,11 +659,7 @@ def gb300_arm(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         g.calc_greens_func(th_host.numpy(), pkg.PREC_FP64, out=out_host.numpy())
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world, dev)
     same = bool(torch.equal(out_host[:4], out[:4].cpu()))
     del out_host
 
