@@ -182,3 +182,47 @@ def test_slip_gradient_matches_finite_differences(orc, name):
             tol = 1e-8 * scale + 1e-14 * (abs(gamma * lik) + abs(pri)) / 1e-4
             print(name, gamma, "max |fd - grad|", np.abs(fd - grad).max(), "scale", scale, "tol", tol)
             assert np.abs(fd - grad).max() <= tol
+
+
+def test_resampling_recurrence_telescopes_to_a_floor_of_the_prefix_sum(orc):
+    """The residual-systematic recurrence of slip_resample_particles
+    (smc_slip.f90:572-589: u = u0/N, a_i = floor((w_i - u) N) + 1,
+    u += a_i/N - w_i), run in binary128 by the oracle, against its exact
+    closed form A_i = floor(N S_i - u0) + 1 for the running count A_i and the
+    running weight S_i, evaluated in exact rational arithmetic.  Random inputs
+    lie far from the near-ties where binary128 rounding could decide, so the
+    counts must agree exactly (and sum to N for normalised weights)."""
+    from fractions import Fraction
+    import math
+    rng = np.random.default_rng(17)
+    for trial in range(24):
+        n = int(rng.integers(2, 600))
+        w = rng.exponential(1.0, n) ** (1 + 3 * rng.random())
+        w = w / w.sum()
+        u0 = float(rng.uniform(1e-5, 1.0))
+        got = orc.resample(w, u0, 0.0)
+        S, A_prev, want = Fraction(0), 0, []
+        for wi in w:
+            S += Fraction(wi)
+            A = math.floor(n * S - Fraction(u0)) + 1
+            want.append(A - A_prev)
+            A_prev = A
+        assert got.tolist() == want, trial
+        assert abs(int(got.sum()) - n) <= 1   # the float weights sum to 1 within rounding
+
+
+def test_greens_invariant_under_a_full_turn_of_strike(orc):
+    """calc_greens_func (gfunc.f90:242-348) depends on the strike only through
+    its sine and cosine: a geometry and its copy with strike + 360 degrees give
+    the same Green's matrix to rounding."""
+    from smc_inversion_fort_gb300.configs import make_stations, preset, random_thetas
+    w = preset("c0")
+    obs = make_stations(w, np.random.default_rng(3))
+    obs["dvec"] = np.zeros(len(obs["obs_sigma"]))
+    o = orc.Oracle(w.settings, obs)
+    for th in random_thetas(w, 3, seed=9):
+        t2 = th.copy()
+        t2[5] += 360.0
+        a, b = o.greens(th), o.greens(t2)
+        scale = np.abs(a).max()
+        assert np.abs(a - b).max() <= 1e-11 * scale
