@@ -12,7 +12,7 @@
 // draws are addressed by (stage, purpose, child index, dimension), so the
 // slot schedule does not change results.
 //
-// Three step engines share the stage-level code (bisection, normalisation,
+// Four step engines share the stage-level code (bisection, normalisation,
 // moments, resampling counts, parent queue, step-size tuning):
 //
 //  * CUDA cores (FP64 up to D = 128; MIXED up to 192 on request): every warp
@@ -24,11 +24,13 @@
 //  * Warp-level tensor-core MMA (MIXED default, D <= 256): M and the slots'
 //    offsets from the stage mean are split into BF16 hi + lo and multiplied
 //    with mma.sync m16n8k16 as lo*hi + hi*lo + hi*hi in three FP32 chains;
-//    each warp owns (16-row, 8-slot) tiles of a 16-warp (or 8-warp, two
-//    geometries per CTA) group.  Up to D = 128 M sits in shared memory (in
-//    registers for the stage when it is small); above, M is kept in global
-//    memory in fragment order and every warp streams its rows through a
-//    cp.async ring (Layout::AGL).
+//    each warp owns (16-row, 8-slot) tiles of a 16-warp group (one geometry
+//    per CTA), an 8-warp group (two per CTA) or, up to D = 64, a 4-warp group
+//    of 16 slots (four per CTA, ENG_MMAQ: the Gram matrix of the end-point
+//    energies then comes from global memory).  Up to D = 128 M sits in shared
+//    memory (in registers for the stage when it is small); above, M is kept in
+//    global memory in fragment order and every warp streams its rows through
+//    a cp.async ring (Layout::AGL).
 //
 //  * tcgen05 (MIXED, D <= 128, on request): one warpgroup per geometry.  M
 //    is split into BF16 hi + lo (stacked 128/DP times to fill the 128-row
@@ -36,6 +38,11 @@
 //    hi*hi + hi*lo + lo*hi as tcgen05.mma (M = 128, N = 2048/DP slots, K = 16
 //    per instruction) into a tensor-memory accumulator, and every thread
 //    reads back its row (one dimension) for 16 slots with tcgen05.ld.
+//
+//  * Global matrix (both precisions, any D up to 1024; one geometry per CTA of
+//    16 warps): M lives in global memory, column-major, and every step streams
+//    it once for the group's 16 slots; each thread owns rows of M and streams
+//    its own entries through a private cp.async ring (gl_gemm).
 //
 // The tensor-core gradient error is O(2^-16) relative; the Metropolis test
 // is exact for any deterministic gradient, and the end-point energies keep
